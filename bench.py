@@ -1,0 +1,392 @@
+"""Benchmark: MLUPS of the fused D2Q9 step on the 8192 x 2048 cylinder
+channel (the roofline configuration), as a fraction of measured HBM
+bandwidth, next to the CPU restatement of the reference timed on the host.
+
+A "step" is one lattice-Boltzmann time step over the whole lattice.
+  value  : lattice updates/s with the state resident in HBM (K fused launches)
+  e2e    : the same through the drop-in API from host buffers: upload rho/u,
+           init_LBM, FusedSolver.step(K), read rho/u back
+  --impl reference : the oracle (C++ restatement of taichi-lbm's unfused
+           kernels, in the reference's call order) on the host cores
+
+Multi-GPU: replicas only (independent lattices, no collective); value = sum
+of all ranks' updates / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "taichi-lbm_gb300")
+for _p in (PKG, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "MLUPS"
+# algorithmic bytes per lattice update: 9 populations read + 9 written
+BYTES_PER_LU = {"fp32": 72, "fp16s": 36, "bf16s": 36}
+CONFIG = {"nx": 8192, "ny": 2048, "radius": 200.0, "cx": 1600.0, "cy": 1024.0, "tau": 0.52,
+          "umax": 0.04}
+MRT_S = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1.0 / 0.52, 1.0 / 0.52]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--model", default="bgk", choices=["bgk", "trt", "mrt"])
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "bf16s"])
+    ap.add_argument("--nx", type=int, default=CONFIG["nx"])
+    ap.add_argument("--ny", type=int, default=CONFIG["ny"])
+    ap.add_argument("--nodes-per-thread", type=int, default=None)
+    ap.add_argument("--no-extras", action="store_true", help="skip the per-model/storage lines")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def workload_config(a):
+    nx, ny = a.nx, a.ny
+    s = nx / CONFIG["nx"]
+    return {"nx": nx, "ny": ny, "radius": CONFIG["radius"] * s, "cx": CONFIG["cx"] * s,
+            "cy": CONFIG["cy"] * ny / CONFIG["ny"], "tau": CONFIG["tau"], "umax": CONFIG["umax"]}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(model, storage):
+    """dram bytes per launch of the fused kernel from the committed ncu
+    summary (profiles/), scaled to the full lattice there; None if absent."""
+    path = os.path.join(ROOT, "profiles", f"fused_{model}_{storage}_cylinder.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_lattice:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def dist_setup():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        rank = int(os.environ["RANK"])
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, ws, local, dist
+    torch.cuda.set_device(0)
+    return 0, 1, 0, None
+
+
+def max_over_ranks(v, dist):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    import torch
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def build(tl, cfg, model, storage, V):
+    from taichi_lbm.workloads import cylinder_channel
+    lb, me, coll, be = cylinder_channel(tl, cfg["nx"], cfg["ny"], cfg["radius"], cfg["cx"], cfg["cy"],
+                                        cfg["tau"], cfg["umax"], model=model,
+                                        mrt_s=MRT_S if model == "mrt" else None, keep_init=False)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, nodes_per_thread=V)
+    return lb, me, coll, be, solver
+
+
+def time_resident(solver, K, W, dist, gpu_index):
+    """K fused launches on the resident state, CUDA events on the launching stream."""
+    import torch
+    solver.begin()
+    solver.run(W)
+    barrier(dist)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(gpu_index) as clk:
+        barrier(dist)
+        e0.record(s)
+        solver.run(K)
+        e1.record(s)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    barrier(dist)
+    solver.finish()
+    return ms, clk.summary()
+
+
+def time_e2e(lb, coll, solver, K, dist):
+    """Drop-in API from host buffers: pinned rho/u upload, init_LBM, step(K),
+    rho/u download; host wall clock with device syncs on both sides."""
+    import torch
+    nx, ny = lb.NX, lb.NY
+    active = coll.group.nodes
+    rho0 = torch.zeros((nx, ny, 1), dtype=torch.float32).pin_memory()
+    rho0[active[:, 0], active[:, 1], 0] = 1.0
+    vel0 = torch.zeros((nx, ny, 2), dtype=torch.float32).pin_memory()
+    rho_out = torch.empty_like(rho0).pin_memory()
+    vel_out = torch.empty_like(vel0).pin_memory()
+    barrier(dist)
+    t0 = time.perf_counter()
+    lb.rho.from_torch(rho0)
+    lb.vel.from_torch(vel0)
+    lb.init_LBM(coll, coll.group)
+    solver.step(K)
+    rho_out.copy_(lb.rho.to_torch(), non_blocking=True)
+    vel_out.copy_(lb.vel.to_torch(), non_blocking=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    barrier(dist)
+    if not torch.isfinite(rho_out).all():
+        raise RuntimeError("non-finite density after the e2e run")
+    h2d = rho0.numel() * 4 + vel0.numel() * 4
+    d2h = rho_out.numel() * 4 + vel_out.numel() * 4
+    return dt, h2d, d2h
+
+
+def cpu_baseline(cfg, model, seconds):
+    """The oracle (unfused reference order, OpenMP over all host cores) on
+    the same lattice for about `seconds` of work."""
+    from oracle import oracle as O
+    from oracle.workloads import cylinder_channel_case
+    meta, arrays = cylinder_channel_case(cfg["nx"], cfg["ny"], cfg["radius"], cfg["cx"], cfg["cy"],
+                                         cfg["tau"], cfg["umax"], model=model,
+                                         mrt_s=MRT_S if model == "mrt" else None)
+    run = O.prepare(meta, arrays)
+    run.step(1)  # warm-up (first touch of every page)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        run.step(1)
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
+    run.o.close()
+    active = arrays["g_fluid"].shape[0]
+    return {"value": active * n / dt / 1e6, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n} steps of the full {cfg['nx']}x{cfg['ny']} lattice ({active} updated nodes) "
+                      f"in {dt:.1f} s; CPU restatement of the reference's unfused kernels, "
+                      "OpenMP over all host cores (Taichi cannot be installed here)"}
+
+
+def run_ours(a):
+    import numpy as np  # noqa: F401
+    import torch
+    import taichi_lbm as tl
+    rank, ws, local, dist = dist_setup()
+    cfg = workload_config(a)
+    K, W = a.steps, max(3, a.warmup)
+    peak, peak_kind = measured_peak()
+    lb, me, coll, be, solver = build(tl, cfg, a.model, a.storage, a.nodes_per_thread)
+    active = coll.group.n
+    ms, clocks = time_resident(solver, K, W, dist, local)
+    ms = max_over_ranks(ms, dist)
+    mlups = active * K * ws / (ms * 1e-3) / 1e6
+    launch_ms = ms / K
+    achieved = BYTES_PER_LU[a.storage] * active / (launch_ms * 1e-3) / 1e9
+    traffic = profile_traffic(a.model, a.storage)
+    e2e_dt, h2d, d2h = time_e2e(lb, coll, solver, K, dist)
+    e2e_dt = max_over_ranks(e2e_dt, dist)
+    line = {
+        "metric": METRIC, "value": round(mlups, 1), "unit": METRIC, "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": round(ms / K, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if a.storage == "fp32" else f"f32 compute, {a.storage} storage",
+        "data": "synthetic (cylinder channel, rho=1, u=0 start)",
+        "config": {"workload": f"cylinder channel {cfg['nx']}x{cfg['ny']}, r={cfg['radius']:g} at "
+                               f"({cfg['cx']:g},{cfg['cy']:g}), {a.model.upper()} tau={cfg['tau']}, "
+                               f"parabolic inlet u_max={cfg['umax']}, PressureNEEM outlet, "
+                               "bounce-back walls", "nodes": cfg["nx"] * cfg["ny"],
+                   "updated_nodes_per_step": active, "model": a.model, "storage": a.storage,
+                   "nodes_per_thread": solver.V, "parallelism": f"replicas x{ws}",
+                   "l2": "state (2 x 9 populations) larger than L2; no flush needed"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "algorithmic_bytes_per_launch": BYTES_PER_LU[a.storage] * active,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "clocks": clocks,
+        "e2e": {"value": round(active * K * ws / e2e_dt / 1e6, 1), "unit": METRIC,
+                "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
+                "seconds": round(e2e_dt, 4),
+                "what": "upload rho/u from pinned host memory, init_LBM, FusedSolver.step(K), "
+                        "download rho/u (the inputs and result are per run; bytes are per step)"},
+        "gpu_launches": K,
+    }
+    del solver, lb, me, coll, be
+    torch.cuda.empty_cache()
+    if not a.no_extras and ws == 1:
+        extras = {}
+        for model, storage in (("trt", "fp32"), ("mrt", "fp32"), ("bgk", "fp16s"), ("bgk", "bf16s")):
+            if (model, storage) == (a.model, a.storage):
+                continue
+            lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None)
+            k2 = max(10, K // 4)
+            ms2, _ = time_resident(s2, k2, W, None, local)
+            act = coll2.group.n
+            gbs = BYTES_PER_LU[storage] * act / (ms2 / k2 * 1e-3) / 1e9
+            extras[f"{model}_{storage}"] = {"MLUPS": round(act * k2 / (ms2 * 1e-3) / 1e6, 1),
+                                            "GB_s": round(gbs, 1), "frac": round(gbs / peak, 4),
+                                            "steps": k2}
+            del s2, lb2, coll2
+            torch.cuda.empty_cache()
+        line["models"] = extras
+    if rank == 0 and ws == 1 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(cfg, a.model, a.cpu_seconds)
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(a):
+    """The reference path on the host cores: taichi-lbm's own Taichi code
+    cannot be installed here (no package, no network), so its C++
+    restatement (oracle/, same unfused kernels in the reference's call order)
+    runs instead, OpenMP over every host core.  Each step is one time step of
+    a band of the same channel, sized from a calibration step so the whole
+    run stays within a few minutes."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from oracle.workloads import cylinder_channel_case
+    cfg = workload_config(a)
+    K, W = a.steps, max(3, a.warmup)
+    budget_s = 150.0
+
+    def case(ny):
+        c = dict(cfg, ny=ny, cy=ny / 2.0 - 0.5, radius=min(cfg["radius"], ny / 4.0))
+        return cylinder_channel_case(c["nx"], c["ny"], c["radius"], c["cx"], c["cy"], c["tau"],
+                                     c["umax"], model=a.model,
+                                     mrt_s=MRT_S if a.model == "mrt" else None)
+
+    # calibrate on a 256-row band, then size the band for the budget
+    meta, arrays = case(256)
+    run = O.prepare(meta, arrays)
+    run.step(1)
+    t0 = time.perf_counter()
+    run.step(2)
+    per_node = (time.perf_counter() - t0) / 2 / (cfg["nx"] * 256)
+    run.o.close()
+    ny = int(budget_s / max(K + W, 1) / per_node / cfg["nx"])
+    ny = max(64, min(cfg["ny"], ny // 32 * 32))
+    meta, arrays = case(ny)
+    run = O.prepare(meta, arrays)
+    run.step(W)
+    t0 = time.perf_counter()
+    run.step(K)
+    dt = time.perf_counter() - t0
+    run.o.close()
+    active = arrays["g_fluid"].shape[0]
+    mlups = active * K / dt / 1e6
+    sample = (f"{K} steps of a {cfg['nx']}x{ny} band of the channel ({active} updated nodes per "
+              "step); C++ restatement of the reference's unfused kernels (Taichi unavailable), "
+              "OpenMP over all host cores")
+    line = {"impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": METRIC,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": K, "warmup": W,
+            "ms_per_step": round(dt / K * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (cylinder channel)",
+            "config": {"workload": f"cylinder channel band {cfg['nx']}x{ny}, {a.model.upper()} "
+                                   f"tau={cfg['tau']}", "model": a.model},
+            "cpu_baseline": {"value": round(mlups, 2), "unit": METRIC, "cores": os.cpu_count(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(mlups, 2), "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

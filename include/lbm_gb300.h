@@ -1,0 +1,275 @@
+/*
+ * lbm_gb300.h — C ABI of the GB300 (sm_103a) D2Q9 lattice-Boltzmann step.
+ *
+ * This is the boundary the Python drop-in (package taichi_lbm) binds through
+ * ctypes.  taichi-lbm itself has no FFI: every per-step operation is a Taichi
+ * @ti.kernel method.  Each entry point below replaces one of those methods and
+ * names it (file:line inside the taichi-lbm project).
+ *
+ * Conventions
+ *  - Every call returns int: LBM_OK (0) or a negative LBM_ERR_*; the message
+ *    of the last failure on the calling thread is read with lbm_last_error().
+ *    No C++ exception crosses this boundary.
+ *  - All buffers are DEVICE pointers owned by the caller (PyTorch allocates
+ *    and frees them); the library never frees caller memory.
+ *  - Work is enqueued on the given CUDA stream (cudaStream_t passed as
+ *    void*; NULL = legacy default stream) and is stream-ordered: calls on one
+ *    stream run in call order, nothing here synchronizes the host.
+ *  - A plan (LbmPlan) is used by one host thread at a time.
+ *
+ * Lattice layout (structure of arrays, x fastest, rows padded):
+ *  node (i, j) of a scalar field is at  j*pitch + i,  0 <= i < nx, 0 <= j < ny
+ *  population k of node (i, j) is at    k*ny*pitch + j*pitch + i
+ *  vector component c is at             c*ny*pitch + j*pitch + i
+ *  psi (one-node halo) of node (i, j) at (j+1)*psi_pitch + (i+1), -1 <= i <= nx,
+ *  -1 <= j <= ny.  pitch and psi_pitch are multiples of 32 elements and the
+ *  base pointers are 128-byte aligned.
+ *  Velocity set (c_k) and weights follow taichi_lbm/lbm.py:44-45:
+ *  k: 0 (0,0) 1 (1,0) 2 (0,1) 3 (-1,0) 4 (0,-1) 5 (1,1) 6 (-1,1) 7 (-1,-1) 8 (1,-1)
+ *
+ *  Groups are the reference's MaskAndGroup node lists
+ *  (taichi_lbm/BoundaryCondition.py:8-12): int32 pairs (i, j), n entries.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_GB300_ABI_VERSION 1
+
+enum {
+  LBM_OK = 0,
+  LBM_ERR_ARG = -1,         /* invalid argument or size */
+  LBM_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+  LBM_ERR_UNSUPPORTED = -3, /* combination this build does not run */
+  LBM_ERR_STATE = -4        /* call out of order (e.g. plan not bound) */
+};
+
+/* collision models (taichi_lbm/CollisionEngine.py) */
+enum { LBM_BGK = 0, LBM_TRT = 1, LBM_MRT = 2 };
+/* fluid models (taichi_lbm/FluidModels.py) */
+enum { LBM_NEWTONIAN = 0, LBM_POWERLAW = 1 };
+/* population storage for the fused path */
+enum { LBM_STORE_F32 = 0, LBM_STORE_F16S = 1, LBM_STORE_BF16S = 2 };
+/* pseudopotentials (taichi_lbm/EOS.py) */
+enum { LBM_EOS_SC = 0, LBM_EOS_VDW = 1, LBM_EOS_RK = 2, LBM_EOS_PR = 3, LBM_EOS_CS = 4 };
+/* boundary-condition kinds (taichi_lbm/BoundaryCondition.py) */
+enum {
+  LBM_BC_FLUID = 0,         /* FluidBoundary, BoundaryCondition.py:452-455 (no-op)     */
+  LBM_BC_VELOCITY_BB = 1,   /* VelocityBB, BoundaryCondition.py:80-102                  */
+  LBM_BC_VELOCITY_EQ = 2,   /* VelocityEquilibrium, BoundaryCondition.py:132-147        */
+  LBM_BC_VELOCITY_NEEM = 3, /* VelocityNEEM, BoundaryCondition.py:149-166               */
+  LBM_BC_PRESSURE_ABC = 4,  /* PressureABC, BoundaryCondition.py:177-205                */
+  LBM_BC_PRESSURE_NEEM = 5, /* PressureNEEM, BoundaryCondition.py:209-226               */
+  LBM_BC_OPEN_NEUMANN = 6,  /* OpenNeumann, BoundaryCondition.py:315-334                */
+  LBM_BC_OPEN_CONV1 = 7,    /* OpenConvective1order, BoundaryCondition.py:337-359       */
+  LBM_BC_OPEN_CONV2 = 8,    /* OpenConvective2order, BoundaryCondition.py:362-390       */
+  LBM_BC_OPEN_EXTRAP = 9,   /* OpenExtrapolation, BoundaryCondition.py:394-411          */
+  LBM_BC_PERIODIC = 10,     /* PeriodicAllBoundary, BoundaryCondition.py:419-432        */
+  LBM_BC_INSIDE = 11,       /* InsideBoundary, BoundaryCondition.py:435-449             */
+  LBM_BC_BOUNCEBACK = 12    /* BounceBackWall, BoundaryCondition.py:231-259             */
+};
+
+/* Lattice fields — the device-side LBField (taichi_lbm/lbm.py:5-56), single
+ * component.  Unused pointers may be NULL for calls that do not touch them. */
+typedef struct LbmLattice {
+  int32_t nx, ny;
+  int32_t pitch;      /* elements per row of every [ny][pitch] plane        */
+  int32_t psi_pitch;  /* elements per row of psi (ny+2 rows)               */
+  float* f;           /* [9][ny][pitch] populations (post-stream)          */
+  float* f2;          /* [9][ny][pitch] populations (post-collision)       */
+  float* rho;         /* [ny][pitch]                                        */
+  float* total_rho;
+  float* pressure;
+  float* total_pressure;
+  float* shear_rate;
+  float* temperature; /* LBField.T                                          */
+  float* vel;         /* [2][ny][pitch]                                     */
+  float* body_force;
+  float* sc_force;    /* LBField.SCforce                                    */
+  float* psi;         /* ShanChenModel.psi_field, one-node halo             */
+  int32_t* mask;      /* [ny][pitch] 1 fluid, -1 solid                      */
+  uint16_t* links;    /* [ny][pitch] LBField.neighbor in bit form: bit k set
+                         = link k has a source (neighbor != -1); bit 15 set =
+                         node was classified (non-solid at classify time)   */
+  float gravity[2];   /* LBField.gravity_force                              */
+} LbmLattice;
+
+/* Collision operator state (taichi_lbm/CollisionEngine.py:6-451). */
+typedef struct LbmCollision {
+  int32_t model;        /* LBM_BGK / LBM_TRT / LBM_MRT                           */
+  int32_t fluid_model;  /* LBM_NEWTONIAN / LBM_POWERLAW                          */
+  float nu;             /* shearviscosity[0] (and NewtonianFluid.nu)              */
+  float nu_bulk;        /* bulkviscosity[0] (MRT)                                 */
+  float magic;          /* magic[0] (TRT)                                         */
+  float tau_min, tau_max;  /* Collision.tau_min / tau_max (CollisionEngine.py:10-11) */
+  float pl_m, pl_n;     /* PowerLawFluid.m / .n (FluidModels.py:20-29)            */
+  float* tau;           /* BGK   [ny][pitch]                                      */
+  float* tau_sym;       /* TRT   [ny][pitch]                                      */
+  float* tau_antisym;   /* TRT   [ny][pitch]                                      */
+  float* diag;          /* MRT   [9][ny][pitch]                                   */
+  float m_inverse[81];  /* MRT   MRTCollision.M_inverse, row-major                */
+} LbmCollision;
+
+/* Pseudopotential parameters (taichi_lbm/EOS.py:5-95). */
+typedef struct LbmEos {
+  int32_t kind;         /* LBM_EOS_*                                              */
+  float a, b, R, G;     /* Pseudopotential a, b, R, G                             */
+  float rho0;           /* SC_psi rho0                                            */
+  float omega;          /* PR_psi omega                                           */
+  float T_cr;           /* temperature_cr                                         */
+} LbmEos;
+
+/* One boundary condition (taichi_lbm/BoundaryCondition.py:57-226, 264-449). */
+typedef struct LbmBoundary {
+  int32_t kind;         /* LBM_BC_*                                               */
+  int32_t direction;    /* PlaneBoundary.direction (1..4)                         */
+  float rho_value;      /* PressureBoundary.rho_value                             */
+  float velocity[2];    /* VelocityBoundary.velocity_value                        */
+  const float* velocity_per_node; /* n x 2 per-node values (group order) or NULL:
+                                     the BoundarySpec.value_fn extension        */
+  float g_coh;          /* OpenConvective2order: ShanChenForceC1.g_coh            */
+  LbmEos eos;           /* OpenConvective2order: the psi model                    */
+} LbmBoundary;
+
+/* ---------------------------------------------------------------- library */
+int lbm_abi_version(void);
+/* Copy the calling thread's last error message into buf (always terminated). */
+int lbm_last_error(char* buf, int64_t buflen);
+
+/* ------------------------------------------------------- per-stage kernels
+ * One launch each, over the given group, exactly the reference method's
+ * effect on the fields.                                                      */
+
+/* LBField.neighbor_classify — taichi_lbm/lbm.py:127-142 */
+int lbm_neighbor_classify(const LbmLattice* lat, void* stream);
+/* LBField.init_LBM — taichi_lbm/lbm.py:119-125 (f = f2 = feq(rho, vel)) */
+int lbm_init_feq(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.density — taichi_lbm/lbm.py:153-164 */
+int lbm_density(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.pressure0 / pressure1 — taichi_lbm/lbm.py:166-182 */
+int lbm_pressure(const LbmLattice* lat, const int32_t* group, int64_t n, int32_t with_sc,
+                 float g_coh, void* stream);
+/* MacroscopicEngine.force_density — taichi_lbm/lbm.py:215-220 */
+int lbm_force_density(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.velocity — taichi_lbm/lbm.py:223-237 */
+int lbm_velocity(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
+
+/* {BGK,TRT,MRT}Collision.initTau — CollisionEngine.py:65-70, 149-155, 301-318 */
+int lbm_collision_init_tau(const LbmLattice* lat, const LbmCollision* c, const int32_t* group,
+                           int64_t n, void* stream);
+/* {BGK,TRT,MRT}Collision.shear_rate — CollisionEngine.py:80-92, 166-178, 332-377 */
+int lbm_collision_shear_rate(const LbmLattice* lat, const LbmCollision* c, const int32_t* group,
+                             int64_t n, void* stream);
+/* {BGK,TRT,MRT}Collision.relaxation_time — CollisionEngine.py:72-78, 157-164, 322-329 */
+int lbm_collision_relaxation_time(const LbmLattice* lat, const LbmCollision* c,
+                                  const int32_t* group, int64_t n, void* stream);
+/* {BGK,TRT,MRT}Collision.apply — CollisionEngine.py:96-110, 223-245, 424-451 */
+int lbm_collision_apply(const LbmLattice* lat, const LbmCollision* c, const int32_t* group,
+                        int64_t n, void* stream);
+
+/* ShanChenForceC1.update_psi — taichi_lbm/ExternalForce.py:137-142 */
+int lbm_sc_update_psi(const LbmLattice* lat, const LbmEos* eos, const int32_t* group, int64_t n,
+                      void* stream);
+/* ShanChenForceC1.cau_SCforce — taichi_lbm/ExternalForce.py:145-158 */
+int lbm_sc_force(const LbmLattice* lat, float g_coh, const int32_t* group, int64_t n, void* stream);
+/* PeriodicPsi_LR (axis 0) / PeriodicPsi_BT (axis 1) — SCBoundaryCondition.py:365-383 */
+int lbm_psi_periodic(const LbmLattice* lat, int32_t axis, void* stream);
+/* FixedPsi.apply — SCBoundaryCondition.py:352-362 */
+int lbm_psi_fixed(const LbmLattice* lat, const int32_t* group, int64_t n, float value, void* stream);
+
+/* <BoundaryCondition>.apply for every kind in LBM_BC_* —
+ * taichi_lbm/BoundaryCondition.py:85-449 (see the enum for each kind's lines) */
+int lbm_boundary_apply(const LbmLattice* lat, const LbmBoundary* bc, const int32_t* group,
+                       int64_t n, void* stream);
+
+/* ----------------------------------------------------------- fused plan
+ * The whole step composed the way the reference's example drivers compose it
+ * (cases/Circular cylinder.py:182-193; cases/Power Law Fluid.py:160-173):
+ * density -> pressure -> force_density -> velocity -> [shear_rate ->
+ * relaxation_time] -> collision.apply -> boundary conditions in insertion
+ * order, as ONE pull-scheme kernel per time step.  The fused state is the
+ * post-collision population set (f2); launch n streams and applies the
+ * boundary conditions of step n-1, then computes the moments and collides
+ * step n.  The first collision and the last stream/boundary pass are done by
+ * the per-stage kernels above (the host wrapper sequences them).           */
+
+#define LBM_MAX_BC 16
+#define LBM_MAX_PROG 64
+#define LBM_PROG_LEN 4
+
+/* Per-node code (uint16) of the fused path:
+ *  bits 0-7  : link k = bit+1 bounces back (source is the node itself, opposite
+ *              population) instead of streaming from (i - cx_k, j - cy_k)
+ *  bit 8     : node collides (member of the collision group)
+ *  bit 9     : node's moments are saved for next step's boundary conditions
+ *  bits 10-15: boundary program id (0 = none), an index into LbmPlanDesc.prog */
+#define LBM_CODE_ACTIVE 0x100u
+#define LBM_CODE_SAVE 0x200u
+#define LBM_CODE_PROG_SHIFT 10
+
+typedef struct LbmPlanDesc {
+  int32_t nx, ny, pitch;
+  int32_t model;        /* LBM_BGK / LBM_TRT / LBM_MRT                      */
+  int32_t fluid_model;  /* LBM_NEWTONIAN / LBM_POWERLAW                     */
+  int32_t storage;      /* LBM_STORE_*                                      */
+  int32_t nodes_per_thread; /* 1, 2 or 4 (x-consecutive nodes per thread) */
+  float tau;            /* Newtonian: uniform tau (BGK) or tau_sym (TRT)    */
+  float tau_antisym;    /* Newtonian TRT                                    */
+  float magic;          /* TRT magic (power law)                            */
+  float tau_min, tau_max, pl_m, pl_n;
+  float mrt_s[9];       /* MRT diag (uniform over the collision group)      */
+  float gravity[2];     /* body force per node: rho/total_rho * gravity     */
+  int32_t nbc;
+  LbmBoundary bc[LBM_MAX_BC];      /* rewrite boundaries, velocity_per_node
+                                      ignored here (see LbmPlanBuffers)     */
+  int32_t nprog;
+  int8_t prog[LBM_MAX_PROG][LBM_PROG_LEN]; /* bc indices, -1 terminated     */
+} LbmPlanDesc;
+
+typedef struct LbmPlanBuffers {
+  void* fa;             /* [9][ny][pitch] populations, element type per storage */
+  void* fb;
+  float* mom_a;         /* [3][ny][pitch] saved (rho, ux, uy)                */
+  float* mom_b;
+  const uint16_t* code; /* [ny][pitch] node codes                            */
+  const uint8_t* seg_flags; /* [ny][nseg] 0 = every node of the segment plain;
+                               nseg = ceil(nx / (32 * nodes_per_thread))     */
+  const float* bc_vel;  /* [2][ny][pitch] per-node boundary velocity or NULL */
+  float* tau;           /* [ny][pitch] power-law state (BGK tau, TRT tau_sym,
+                           MRT diag[7]) or NULL                              */
+} LbmPlanBuffers;
+
+typedef struct LbmPlan LbmPlan;
+
+int lbm_plan_create(const LbmPlanDesc* desc, LbmPlan** out);
+int lbm_plan_bind(LbmPlan* plan, const LbmPlanBuffers* bufs);
+/* Launch nsteps fused steps, alternating fa/fb and mom_a/mom_b. */
+int lbm_plan_run(LbmPlan* plan, int32_t nsteps, void* stream);
+/* Which buffer holds the current post-collision state: 0 = fa/mom_a, 1 = fb/mom_b. */
+int lbm_plan_get_parity(const LbmPlan* plan, int32_t* parity);
+int lbm_plan_set_parity(LbmPlan* plan, int32_t parity);
+/* Stream + boundary conditions of the last step only: writes the post-stream
+ * populations (fp32, [9][ny][pitch]) into f_out; moments are not computed.  */
+int lbm_plan_stream(LbmPlan* plan, float* f_out, void* stream);
+/* Convert fp32 populations into / out of the plan's current state buffer
+ * (identity copies for fp32 storage, shifted 16-bit for F16S/BF16S).        */
+int lbm_plan_import(LbmPlan* plan, const float* f_post, void* stream);
+int lbm_plan_export(LbmPlan* plan, float* f_post, void* stream);
+int lbm_plan_destroy(LbmPlan* plan);
+
+/* ----------------------------------------------------------- reductions
+ * FP64 sums over the nodes whose code has LBM_CODE_ACTIVE, of the current
+ * population state: out[0] = sum f, out[1] = sum f c_x, out[2] = sum f c_y.
+ * partials: caller scratch of at least lbm_reduce_scratch_doubles() doubles. */
+int64_t lbm_reduce_scratch_doubles(void);
+int lbm_plan_reduce_moments(LbmPlan* plan, double* partials, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

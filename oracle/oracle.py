@@ -153,9 +153,35 @@ def _fluid_model_args(meta):
     return 1, 0.0, float(fm[1]), float(fm[2])
 
 
+class Run:
+    """A prepared oracle lattice: ``step(n)`` runs n reference steps,
+    ``finish()`` runs the next moment prologue and returns the fields."""
+
+    def __init__(self, o, step, moments, extract):
+        self.o, self._step, self._moments, self._extract = o, step, moments, extract
+
+    def step(self, n=1):
+        for _ in range(int(n)):
+            self._step()
+
+    def finish(self):
+        self._moments()
+        out = self._extract()
+        self.o.close()
+        return out
+
+
 def replay(meta, arrays, steps=None, nthreads=None):
     """Run a case description through the oracle; returns a dict of fields
     at the comparison point (after the moment prologue of step steps+1)."""
+    r = prepare(meta, arrays, nthreads)
+    r.step(int(meta["steps"] if steps is None else steps))
+    return r.finish()
+
+
+def prepare(meta, arrays, nthreads=None):
+    """Set a case description up in the oracle (mask, neighbor table,
+    collision state, initial populations) and return a Run."""
     if nthreads is not None:
         os.environ["OMP_NUM_THREADS"] = str(nthreads)
     nx, ny = int(meta["NX"]), int(meta["NY"])
@@ -201,7 +227,6 @@ def replay(meta, arrays, steps=None, nthreads=None):
 
     fk, fnu, fm_m, fm_n = _fluid_model_args(meta)
     kind = meta["step_kind"]
-    nsteps = int(meta["steps"] if steps is None else steps)
 
     uvels = {}
     for b in bcs:
@@ -266,12 +291,15 @@ def replay(meta, arrays, steps=None, nthreads=None):
                 o.call(model + "_relaxation_time", fluid, fk, fnu, fm_m, fm_n, lo, hi)
         o.call(model + "_apply", fluid)
 
-    for _ in range(nsteps):
+    def step():
         moments()
         collide()
         apply_bcs()
-    moments()
 
+    return Run(o, step, moments, lambda: _extract(o, model, sc))
+
+
+def _extract(o, model, sc):
     out = {}
     for name in ("f", "f2", "rho", "total_rho", "vel", "body_force", "total_pressure", "shear_rate",
                  "mask", "neighbor"):
@@ -288,5 +316,4 @@ def replay(meta, arrays, steps=None, nthreads=None):
         out["psi"] = o.field("psi").copy()
         out["sc_force"] = o.field("SCforce").copy()
     out["error"] = o.error()
-    o.close()
     return out

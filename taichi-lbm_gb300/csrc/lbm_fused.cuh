@@ -1,0 +1,529 @@
+// Fused pull-scheme D2Q9 step for sm_103a.
+//
+// One launch = the boundary pass of step n-1 (stream carriers compiled into
+// per-node bounce bits, then the rewrite boundaries in insertion order) and
+// the moments + collision of step n, for the whole lattice.  State between
+// launches is the post-collision population set; see lbm_gb300.h.
+//
+// Work decomposition: one warp owns one row segment of 32*V x-consecutive
+// nodes; each lane owns V nodes.  Population k of the V nodes is fetched with
+// one aligned V-wide load from row (y - cy_k); the x shift by cx_k = +-1 is
+// done with one warp shuffle, lane 0 / lane 31 fetching the single element
+// that crosses the segment edge.  Every population element of the source is
+// therefore read from DRAM once and every output element written once
+// (72 B per fp32 lattice update), with 128-bit loads and stores.
+//
+// Segments whose nodes are all plain (collide, stream all links, no boundary
+// program, no saved moments) skip the per-node code load entirely; the others
+// take the per-node path (bounce-back links, boundary programs, saved moments).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "lbm_common.cuh"
+
+namespace lbm {
+
+struct FusedParams {
+  int nx, ny, pitch, nseg;
+  size_t plane;
+  const void* src;
+  void* dst;
+  const float* mom_in;
+  float* mom_out;
+  const uint16_t* code;
+  const uint8_t* seg_flags;
+  float* tau;
+  int model, fluid_model, has_force;
+  float omega, omega_a, magic, tau_min, tau_max, pl_m, pl_n;
+  float s[9];
+  float gx, gy;
+  int nbc;
+  LbmBoundary bc[LBM_MAX_BC];
+  int8_t prog[LBM_MAX_PROG][LBM_PROG_LEN];
+};
+
+// ------------------------------------------------------------ storage
+template <int ST>
+struct Storage;
+template <>
+struct Storage<LBM_STORE_F32> {
+  using T = float;
+  static __device__ __forceinline__ float dec(T v, float) { return v; }
+  static __device__ __forceinline__ T enc(float v, float) { return v; }
+};
+template <>
+struct Storage<LBM_STORE_F16S> {
+  using T = __half;
+  static __device__ __forceinline__ float dec(T v, float w) { return __half2float(v) + w; }
+  static __device__ __forceinline__ T enc(float v, float w) { return __float2half_rn(v - w); }
+};
+template <>
+struct Storage<LBM_STORE_BF16S> {
+  using T = __nv_bfloat16;
+  static __device__ __forceinline__ float dec(T v, float w) { return __bfloat162float(v) + w; }
+  static __device__ __forceinline__ T enc(float v, float w) { return __float2bfloat16_rn(v - w); }
+};
+
+template <int BYTES>
+struct Raw;
+template <>
+struct Raw<16> { using type = uint4; };
+template <>
+struct Raw<8> { using type = uint2; };
+template <>
+struct Raw<4> { using type = unsigned int; };
+template <>
+struct Raw<2> { using type = unsigned short; };
+
+// Aligned loads/stores of V consecutive elements in pieces of at most 16 B.
+template <typename T, int V>
+__device__ __forceinline__ void load_vec(const T* p, T (&out)[V]) {
+  constexpr int B = sizeof(T) * V > 16 ? 16 : sizeof(T) * V;
+  constexpr int E = B / sizeof(T);
+  using R = typename Raw<B>::type;
+#pragma unroll
+  for (int c = 0; c < V / E; ++c) {
+    R r = __ldg(reinterpret_cast<const R*>(p + c * E));
+    memcpy(&out[c * E], &r, B);
+  }
+}
+template <typename T, int V>
+__device__ __forceinline__ void store_vec(T* p, const T (&in)[V]) {
+  constexpr int B = sizeof(T) * V > 16 ? 16 : sizeof(T) * V;
+  constexpr int E = B / sizeof(T);
+  using R = typename Raw<B>::type;
+#pragma unroll
+  for (int c = 0; c < V / E; ++c) {
+    R r;
+    memcpy(&r, &in[c * E], B);
+    __stcs(reinterpret_cast<R*>(p + c * E), r);
+  }
+}
+template <typename T>
+__device__ __forceinline__ T load1(const T* p) {
+  using R = typename Raw<sizeof(T)>::type;
+  R r = __ldg(reinterpret_cast<const R*>(p));
+  T out;
+  memcpy(&out, &r, sizeof(T));
+  return out;
+}
+
+__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// population k is unknown for a plane boundary of direction dir
+// (BoundaryCondition.py:63-72): exactly the links with c_k . c_dir = -1
+__host__ __device__ constexpr bool is_unknown(int dir, int k) {
+  return CX(k) * CX(dir) + CY(k) * CY(dir) == -1;
+}
+
+// Post-stream populations of node (x, y): the stream carriers' result, read
+// from the post-collision source with the node's bounce bits.
+template <int ST>
+__device__ __forceinline__ void gather_node(const FusedParams& p, int x, int y, float g[9]) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  const unsigned code = p.code[(size_t)y * p.pitch + x];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    if (k > 0 && (code & (1u << (k - 1)))) {
+      g[k] = S::dec(load1(src + OPP(k) * p.plane + (size_t)y * p.pitch + x), W(OPP(k)));
+    } else {
+      const int xs = wrap(x - CX(k), p.nx), ys = wrap(y - CY(k), p.ny);
+      g[k] = S::dec(load1(src + k * p.plane + (size_t)ys * p.pitch + xs), W(k));
+    }
+  }
+}
+
+__device__ __forceinline__ float bc_rhow(int dir, float vx, float vy, const float f[9]) {
+  // BoundaryCondition.py:119-129
+  if (dir == 2) return 1.0f / (1.0f + vy) * (f[0] + f[1] + f[3] + 2.0f * (f[2] + f[5] + f[6]));
+  if (dir == 4) return 1.0f / (1.0f - vy) * (f[0] + f[1] + f[3] + 2.0f * (f[4] + f[7] + f[8]));
+  if (dir == 1) return 1.0f / (1.0f + vx) * (f[0] + f[2] + f[4] + 2.0f * (f[1] + f[5] + f[8]));
+  return 1.0f / (1.0f - vx) * (f[0] + f[2] + f[4] + 2.0f * (f[3] + f[6] + f[7]));
+}
+
+__device__ __forceinline__ bool is_unknown_dyn(int dir, int k) {
+  return CX(k) * cx_dyn(dir) + CY(k) * cy_dyn(dir) == -1;
+}
+
+// One rewrite boundary on node (x, y) whose post-stream populations are f.
+// Moments read from mom_in are the start-of-step values the reference reads
+// (its rho/vel fields still hold them when the boundary pass runs).
+template <int ST>
+__device__ __noinline__ void apply_bc(const FusedParams& p, int bci, int x, int y, float f[9]) {
+  const LbmBoundary& b = p.bc[bci];
+  const int dir = b.direction;
+  const int x2 = x - cx_dyn(dir), y2 = y - cy_dyn(dir);
+  const size_t q = (size_t)y * p.pitch + x, q2 = (size_t)y2 * p.pitch + x2;
+  float Ux = b.velocity[0], Uy = b.velocity[1];
+  if (b.velocity_per_node) {
+    Ux = b.velocity_per_node[q];
+    Uy = b.velocity_per_node[p.plane + q];
+  }
+  switch (b.kind) {
+    case LBM_BC_VELOCITY_EQ: {  // BoundaryCondition.py:137-147
+      const float r = bc_rhow(dir, Ux, Uy, f), uu = Ux * Ux + Uy * Uy;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) f[k] = feq_k(k, r, Ux, Uy, uu);
+      break;
+    }
+    case LBM_BC_VELOCITY_NEEM: {  // BoundaryCondition.py:154-166
+      const float r = bc_rhow(dir, Ux, Uy, f), uu = Ux * Ux + Uy * Uy;
+      float g[9];
+      gather_node<ST>(p, x2, y2, g);
+      const float r2 = p.mom_in[q2], u2x = p.mom_in[p.plane + q2], u2y = p.mom_in[2 * p.plane + q2];
+      const float uu2 = u2x * u2x + u2y * u2y;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) f[k] = feq_k(k, r, Ux, Uy, uu) + g[k] - feq_k(k, r2, u2x, u2y, uu2);
+      break;
+    }
+    case LBM_BC_VELOCITY_BB: {  // BoundaryCondition.py:85-102
+      const float rw = p.mom_in[q];
+#pragma unroll
+      for (int k = 1; k < 9; ++k)
+        if (is_unknown_dyn(dir, k)) f[k] += 6.0f * W(k) * rw * ((float)CX(k) * Ux + (float)CY(k) * Uy);
+      break;
+    }
+    case LBM_BC_PRESSURE_ABC: {  // BoundaryCondition.py:182-205
+      const float ux = 1.5f * p.mom_in[p.plane + q] - 0.5f * p.mom_in[p.plane + q2];
+      const float uy = 1.5f * p.mom_in[2 * p.plane + q] - 0.5f * p.mom_in[2 * p.plane + q2];
+      const float uw2 = ux * ux + uy * uy;
+#pragma unroll
+      for (int k = 1; k < 9; ++k)
+        if (is_unknown_dyn(dir, k)) {
+          const float cu = (float)CX(k) * ux + (float)CY(k) * uy;
+          f[k] = -f[k] + 2.0f * W(k) * b.rho_value * (1.0f + 4.5f * cu * cu - 1.5f * uw2);
+        }
+      break;
+    }
+    case LBM_BC_PRESSURE_NEEM: {  // BoundaryCondition.py:215-226
+      float g[9];
+      gather_node<ST>(p, x2, y2, g);
+      const float r = p.mom_in[q], r2 = p.mom_in[q2];
+      const float ux = p.mom_in[p.plane + q2], uy = p.mom_in[2 * p.plane + q2];
+      const float uu = ux * ux + uy * uy;
+#pragma unroll
+      for (int k = 1; k < 9; ++k)
+        if (is_unknown_dyn(dir, k)) f[k] = feq_k(k, r, ux, uy, uu) + g[k] - feq_k(k, r2, ux, uy, uu);
+      break;
+    }
+    case LBM_BC_OPEN_NEUMANN:  // BoundaryCondition.py:321-334
+    case LBM_BC_OPEN_CONV1: {  // BoundaryCondition.py:342-359
+      float g[9];
+      gather_node<ST>(p, x2, y2, g);
+      float lam = 0.0f;
+      if (b.kind == LBM_BC_OPEN_CONV1) {
+        const float ux = p.mom_in[p.plane + q2], uy = p.mom_in[2 * p.plane + q2];
+        lam = sqrtf(ux * ux + uy * uy);
+      }
+#pragma unroll
+      for (int k = 1; k < 9; ++k)
+        if (is_unknown_dyn(dir, k)) f[k] = b.kind == LBM_BC_OPEN_CONV1 ? (f[k] + lam * g[k]) / (1.0f + lam) : g[k];
+      break;
+    }
+    case LBM_BC_OPEN_EXTRAP: {  // BoundaryCondition.py:400-411
+      float g2[9], g3[9];
+      gather_node<ST>(p, x2, y2, g2);
+      gather_node<ST>(p, x2 - cx_dyn(dir), y2 - cy_dyn(dir), g3);
+#pragma unroll
+      for (int k = 1; k < 9; ++k)
+        if (is_unknown_dyn(dir, k)) f[k] = 2.0f * g2[k] - g3[k];
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+}  // namespace lbm
+
+namespace lbm {
+
+// Relaxation + collision of one node in place; returns the new relaxation
+// state (power law) or the old one.
+template <int MODEL, bool PL>
+__device__ __forceinline__ float relax_collide(const FusedParams& p, float f[9], float rho, float ux, float uy,
+                                               float Fx, float Fy, float state) {
+  if (MODEL == LBM_MRT) {
+    float s[9];
+#pragma unroll
+    for (int a = 0; a < 9; ++a) s[a] = p.s[a];
+    if (PL) {
+      // CollisionEngine.py:332-377 with the previous step's s7 = s8 = state,
+      // then :322-329 for the new rate
+      const float uu = ux * ux + uy * uy;
+      float fn[9], mn[9], mneq[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) fn[k] = f[k] - feq_k(k, rho, ux, uy, uu);
+      mrt_forward(fn, mn);
+      s[7] = s[8] = state;
+#pragma unroll
+      for (int a = 0; a < 9; ++a) mn[a] *= s[a];
+      mrt_backward(mn, mneq);
+      const float gamma = shear_from_neq(mneq, -1.5f / rho);
+      const float t = powerlaw_tau(p.pl_m, p.pl_n, gamma, p.tau_min, p.tau_max);
+      state = 1.0f / t;
+      s[7] = s[8] = state;
+    }
+    collide_mrt(f, rho, ux, uy, Fx, Fy, s, p.has_force);
+    return state;
+  }
+  float om = p.omega, oa = p.omega_a;
+  if (PL) {
+    // CollisionEngine.py:80-92 / 166-178 (previous tau), then :72-78 / 157-164
+    const float uu = ux * ux + uy * uy;
+    float fn[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) fn[k] = f[k] - feq_k(k, rho, ux, uy, uu);
+    const float gamma = shear_from_neq(fn, -1.5f / rho / state);
+    const float t = powerlaw_tau(p.pl_m, p.pl_n, gamma, p.tau_min, p.tau_max);
+    state = t;
+    om = 1.0f / t;
+    if (MODEL == LBM_TRT) oa = 1.0f / (p.magic / (t - 0.5f) + 0.5f);
+  }
+  if (MODEL == LBM_BGK) collide_bgk(f, rho, ux, uy, Fx, Fy, om, p.has_force);
+  else collide_trt(f, rho, ux, uy, Fx, Fy, om, oa, p.has_force);
+  return state;
+}
+
+template <int MODEL, bool PL, int ST, int V>
+__global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= (long long)p.ny * p.nseg) return;  // whole warps only
+  const int y = (int)(warp / p.nseg);
+  const int seg = (int)(warp - (long long)y * p.nseg);
+  const int x0 = seg * 32 * V + lane * V;
+  const bool live = x0 < p.nx;
+  const int ilast = p.nx - 1 - x0;  // index of node nx-1 in this chunk, if in [0, V)
+  const T* src = reinterpret_cast<const T*>(p.src);
+  const size_t rowoff = (size_t)y * p.pitch;
+
+  float f[V][9];
+  // ---- pull-stream gather: one aligned V-wide load per population
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
+    float c[V];
+    if (live) {
+      T raw[V];
+      load_vec<T, V>(row + x0, raw);
+#pragma unroll
+      for (int i = 0; i < V; ++i) c[i] = S::dec(raw[i], W(k));
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) c[i] = 0.0f;
+    }
+    if (CX(k) == 0) {
+#pragma unroll
+      for (int i = 0; i < V; ++i) f[i][k] = c[i];
+    } else if (CX(k) == 1) {
+      float left = __shfl_up_sync(FULL, c[V - 1], 1);
+      if (lane == 0 && live) left = S::dec(load1(row + wrap(x0 - 1, p.nx)), W(k));
+      f[0][k] = left;
+#pragma unroll
+      for (int i = 1; i < V; ++i) f[i][k] = c[i - 1];
+    } else {
+      float right = __shfl_down_sync(FULL, c[0], 1);
+      if (lane == 31 && live) right = S::dec(load1(row + wrap(x0 + V, p.nx)), W(k));
+#pragma unroll
+      for (int i = 0; i < V - 1; ++i) f[i][k] = c[i + 1];
+      f[V - 1][k] = right;
+      if (live && ilast < V) {  // node nx-1 pulls from column 0
+        const float v0 = S::dec(load1(row), W(k));
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+          if (i == ilast) f[i][k] = v0;
+      }
+    }
+  }
+
+  // ---- per-node path: bounce-back links, boundary programs
+  const unsigned flag = p.seg_flags[(size_t)y * p.nseg + seg];
+  unsigned code[V];
+#pragma unroll
+  for (int i = 0; i < V; ++i) code[i] = LBM_CODE_ACTIVE;
+  if (flag) {
+    if (live) {
+      uint16_t raw[V];
+      load_vec<uint16_t, V>(p.code + rowoff + x0, raw);
+#pragma unroll
+      for (int i = 0; i < V; ++i) code[i] = (x0 + i < p.nx) ? raw[i] : 0u;
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) code[i] = 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      if (code[i] & 0xffu) {
+#pragma unroll
+        for (int k = 1; k < 9; ++k)
+          if (code[i] & (1u << (k - 1)))
+            f[i][k] = S::dec(load1(src + (size_t)OPP(k) * p.plane + rowoff + x0 + i), W(OPP(k)));
+      }
+      const unsigned prog = code[i] >> LBM_CODE_PROG_SHIFT;
+      if (prog) {
+        float t[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) t[k] = f[i][k];
+        for (int s = 0; s < LBM_PROG_LEN; ++s) {
+          const int bi = p.prog[prog][s];
+          if (bi < 0) break;
+          apply_bc<ST>(p, bi, x0 + i, y, t);
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) f[i][k] = t[k];
+      }
+    }
+  }
+
+  // ---- moments, relaxation, collision
+  float tau[V];
+  if (PL) {
+    if (live) {
+      load_vec<float, V>(p.tau + rowoff + x0, tau);
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) tau[i] = 1.0f;
+    }
+  }
+  const float Fx = p.has_force ? p.gx : 0.0f, Fy = p.has_force ? p.gy : 0.0f;
+#pragma unroll
+  for (int i = 0; i < V; ++i) {
+    float* fi = f[i];
+    const float rho = ((fi[0] + fi[1]) + (fi[2] + fi[3])) + ((fi[4] + fi[5]) + (fi[6] + fi[7])) + fi[8];
+    const float jx = (fi[1] - fi[3]) + (fi[5] - fi[6]) + (fi[8] - fi[7]);
+    const float jy = (fi[2] - fi[4]) + (fi[5] + fi[6]) - (fi[7] + fi[8]);
+    const float ux = (jx + 0.5f * Fx) / rho, uy = (jy + 0.5f * Fy) / rho;
+    if (flag && (code[i] & LBM_CODE_SAVE)) {
+      const size_t q = rowoff + x0 + i;
+      p.mom_out[q] = rho;
+      p.mom_out[p.plane + q] = ux;
+      p.mom_out[2 * p.plane + q] = uy;
+    }
+    const float st = relax_collide<MODEL, PL>(p, fi, rho, ux, uy, Fx, Fy, PL ? tau[i] : 0.0f);
+    if (!(code[i] & LBM_CODE_ACTIVE)) {
+      // not in the collision group: its post-collision populations never
+      // change (the reference never writes f2 there), so carry them over
+      if (live) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), W(k));
+      }
+    } else if (PL) {
+      tau[i] = st;
+    }
+  }
+  if (!live) return;
+  if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
+  T* dst = reinterpret_cast<T*>(p.dst);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    T raw[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], W(k));
+    store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
+  }
+}
+
+// Stream + boundary pass only (the last half step of a fused run): writes the
+// post-stream populations of every colliding node as fp32.
+template <int ST>
+__global__ void k_stream_only(const FusedParams p, float* fout) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= p.nx) return;
+  const size_t q = (size_t)y * p.pitch + x;
+  const unsigned code = p.code[q];
+  if (!(code & LBM_CODE_ACTIVE)) return;
+  float g[9];
+  gather_node<ST>(p, x, y, g);
+  const unsigned prog = code >> LBM_CODE_PROG_SHIFT;
+  for (int s = 0; prog && s < LBM_PROG_LEN; ++s) {
+    const int bi = p.prog[prog][s];
+    if (bi < 0) break;
+    apply_bc<ST>(p, bi, x, y, g);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) fout[(size_t)k * p.plane + q] = g[k];
+}
+
+template <int ST>
+__global__ void k_convert(const FusedParams p, const float* in, void* out, int to_storage) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const size_t n = 9 * p.plane;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / p.plane);
+    const float w = k == 0 ? W(0) : (k <= 4 ? W(1) : W(5));
+    if (to_storage) reinterpret_cast<T*>(out)[t] = S::enc(in[t], w);
+    else reinterpret_cast<float*>(out)[t] = S::dec(reinterpret_cast<const T*>(p.src)[t], w);
+  }
+}
+
+// FP64 sums of f, f c_x, f c_y over colliding nodes of the state p.src.
+constexpr int REDUCE_BLOCKS = 152 * 4;
+constexpr int REDUCE_TPB = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int ST>
+__global__ void __launch_bounds__(REDUCE_TPB) k_reduce_partial(const FusedParams p, double* partials) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  const size_t n = (size_t)p.ny * p.pitch;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(q % p.pitch);
+    if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
+    float m0 = 0.0f, mx = 0.0f, my = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const float v = S::dec(src[(size_t)k * p.plane + q], W(k));
+      m0 += v;
+      mx += (float)CX(k) * v;
+      my += (float)CY(k) * v;
+    }
+    a0 += m0;
+    a1 += mx;
+    a2 += my;
+  }
+  __shared__ double sh[3][REDUCE_TPB / 32];
+  a0 = warp_sum(a0);
+  a1 = warp_sum(a1);
+  a2 = warp_sum(a2);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = a0;
+    sh[1][w] = a1;
+    sh[2][w] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int i = 0; i < REDUCE_TPB / 32; ++i) s += sh[threadIdx.x][i];
+    partials[(size_t)blockIdx.x * 3 + threadIdx.x] = s;
+  }
+}
+
+template <int ST>
+__global__ void k_reduce_final(const double* partials, int nblocks, double* out) {
+  // one warp per component, fixed order: deterministic
+  const int c = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (c >= 3) return;
+  double s = 0.0;
+  for (int b = l; b < nblocks; b += 32) s += partials[(size_t)b * 3 + c];
+  s = warp_sum(s);
+  if (l == 0) out[c] = s;
+}
+
+}  // namespace lbm

@@ -1,0 +1,3 @@
+// Fused kernels with fp16 shifted storage (f - w_k), fp32 arithmetic.
+#include "lbm_fused_launch.cuh"
+LBM_INSTANTIATE_STORAGE(LBM_STORE_F16S, 4, 8)

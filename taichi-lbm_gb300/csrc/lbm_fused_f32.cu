@@ -1,0 +1,3 @@
+// Fused kernels with fp32 population storage (2 or 4 nodes per thread).
+#include "lbm_fused_launch.cuh"
+LBM_INSTANTIATE_STORAGE(LBM_STORE_F32, 2, 4)

@@ -1,0 +1,205 @@
+// Fused-step plans: validation, buffer binding and stream-ordered launches.
+#include <cstring>
+#include <new>
+
+#include "lbm_fused_launch.cuh"
+
+struct LbmPlan {
+  LbmPlanDesc d;
+  LbmPlanBuffers b;
+  bool bound = false;
+  int parity = 0;
+  lbm::FusedParams base;
+};
+
+namespace {
+
+using lbm::FusedParams;
+
+int storage_bytes(int st) { return st == LBM_STORE_F32 ? 4 : 2; }
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+FusedParams params_for(LbmPlan* pl) {
+  FusedParams p = pl->base;
+  const int cur = pl->parity;
+  p.src = cur ? pl->b.fb : pl->b.fa;
+  p.dst = cur ? pl->b.fa : pl->b.fb;
+  p.mom_in = cur ? pl->b.mom_b : pl->b.mom_a;
+  p.mom_out = cur ? pl->b.mom_a : pl->b.mom_b;
+  p.code = pl->b.code;
+  p.seg_flags = pl->b.seg_flags;
+  p.tau = pl->b.tau;
+  return p;
+}
+
+int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s) {
+  switch (st) {
+    case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, V, s);
+    case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, V, s);
+    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, V, s);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
+  if (!d || !out) return lbm_err::set(LBM_ERR_ARG, "plan_create: NULL argument");
+  *out = nullptr;
+  if (d->nx <= 0 || d->ny <= 0) return lbm_err::set(LBM_ERR_ARG, "lattice %d x %d", d->nx, d->ny);
+  if (d->pitch < d->nx || d->pitch % 32)
+    return lbm_err::set(LBM_ERR_ARG, "pitch %d must be >= nx and a multiple of 32", d->pitch);
+  if (d->model < LBM_BGK || d->model > LBM_MRT) return lbm_err::set(LBM_ERR_ARG, "model %d", d->model);
+  if (d->fluid_model != LBM_NEWTONIAN && d->fluid_model != LBM_POWERLAW)
+    return lbm_err::set(LBM_ERR_ARG, "fluid model %d", d->fluid_model);
+  if (d->storage < LBM_STORE_F32 || d->storage > LBM_STORE_BF16S)
+    return lbm_err::set(LBM_ERR_ARG, "storage %d", d->storage);
+  const int V = d->nodes_per_thread;
+  const bool vok = d->storage == LBM_STORE_F32 ? (V == 2 || V == 4) : (V == 4 || V == 8);
+  if (!vok) return lbm_err::set(LBM_ERR_UNSUPPORTED, "nodes_per_thread %d for storage %d", V, d->storage);
+  if (d->nbc < 0 || d->nbc > LBM_MAX_BC) return lbm_err::set(LBM_ERR_ARG, "nbc %d", d->nbc);
+  if (d->nprog < 0 || d->nprog > LBM_MAX_PROG) return lbm_err::set(LBM_ERR_ARG, "nprog %d", d->nprog);
+  for (int i = 0; i < d->nbc; ++i) {
+    const LbmBoundary& b = d->bc[i];
+    if (b.kind < LBM_BC_VELOCITY_BB || b.kind > LBM_BC_OPEN_EXTRAP || b.kind == LBM_BC_OPEN_CONV2)
+      return lbm_err::set(LBM_ERR_UNSUPPORTED, "boundary kind %d has no fused form", b.kind);
+    if (b.direction < 1 || b.direction > 4)
+      return lbm_err::set(LBM_ERR_ARG, "boundary %d direction %d", i, b.direction);
+  }
+  for (int p = 0; p < d->nprog; ++p)
+    for (int s = 0; s < LBM_PROG_LEN; ++s) {
+      const int bi = d->prog[p][s];
+      if (bi >= d->nbc) return lbm_err::set(LBM_ERR_ARG, "program %d names boundary %d", p, bi);
+    }
+  LbmPlan* pl = new (std::nothrow) LbmPlan();
+  if (!pl) return lbm_err::set(LBM_ERR_ARG, "out of host memory");
+  pl->d = *d;
+  FusedParams& p = pl->base;
+  std::memset(&p, 0, sizeof(p));
+  p.nx = d->nx;
+  p.ny = d->ny;
+  p.pitch = d->pitch;
+  p.nseg = (d->nx + 32 * V - 1) / (32 * V);
+  p.plane = (size_t)d->ny * d->pitch;
+  p.model = d->model;
+  p.fluid_model = d->fluid_model;
+  p.has_force = (d->gravity[0] != 0.0f || d->gravity[1] != 0.0f) ? 1 : 0;
+  p.omega = 1.0f / d->tau;
+  p.omega_a = d->model == LBM_TRT ? 1.0f / d->tau_antisym : 0.0f;
+  p.magic = d->magic;
+  p.tau_min = d->tau_min;
+  p.tau_max = d->tau_max;
+  p.pl_m = d->pl_m;
+  p.pl_n = d->pl_n;
+  for (int a = 0; a < 9; ++a) p.s[a] = d->mrt_s[a];
+  p.gx = d->gravity[0];
+  p.gy = d->gravity[1];
+  p.nbc = d->nbc;
+  std::memcpy(p.bc, d->bc, sizeof(p.bc));
+  std::memcpy(p.prog, d->prog, sizeof(p.prog));
+  *out = pl;
+  return LBM_OK;
+}
+
+int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
+  if (!pl || !b) return lbm_err::set(LBM_ERR_ARG, "plan_bind: NULL argument");
+  if (!b->fa || !b->fb || !b->code || !b->seg_flags)
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: fa, fb, code and seg_flags are required");
+  if (!b->mom_a || !b->mom_b) return lbm_err::set(LBM_ERR_ARG, "plan_bind: moment buffers are required");
+  if (pl->d.fluid_model == LBM_POWERLAW && !b->tau)
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: power law needs the tau state buffer");
+  const size_t va = (size_t)storage_bytes(pl->d.storage) * pl->d.nodes_per_thread;
+  if (!aligned(b->fa, va) || !aligned(b->fb, va) || !aligned(b->code, 16) || (b->tau && !aligned(b->tau, 16)))
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: buffers must be 16-byte aligned");
+  pl->b = *b;
+  pl->bound = true;
+  pl->parity = 0;
+  return LBM_OK;
+}
+
+int lbm_plan_run(LbmPlan* pl, int32_t nsteps, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "plan_run: plan not bound");
+  if (nsteps < 0) return lbm_err::set(LBM_ERR_ARG, "plan_run: nsteps %d", nsteps);
+  for (int32_t s = 0; s < nsteps; ++s) {
+    FusedParams p = params_for(pl);
+    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, (cudaStream_t)stream);
+    if (rc) return rc;
+    pl->parity ^= 1;
+  }
+  return LBM_OK;
+}
+
+int lbm_plan_get_parity(const LbmPlan* pl, int32_t* parity) {
+  if (!pl || !parity) return lbm_err::set(LBM_ERR_ARG, "plan_get_parity: NULL argument");
+  *parity = pl->parity;
+  return LBM_OK;
+}
+
+int lbm_plan_set_parity(LbmPlan* pl, int32_t parity) {
+  if (!pl || (parity != 0 && parity != 1)) return lbm_err::set(LBM_ERR_ARG, "plan_set_parity: bad argument");
+  pl->parity = parity;
+  return LBM_OK;
+}
+
+int lbm_plan_stream(LbmPlan* pl, float* f_out, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "plan_stream: plan not bound");
+  if (!f_out) return lbm_err::set(LBM_ERR_ARG, "plan_stream: f_out is NULL");
+  FusedParams p = params_for(pl);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return lbm::launch_stream_only<LBM_STORE_F32>(p, f_out, s);
+    case LBM_STORE_F16S: return lbm::launch_stream_only<LBM_STORE_F16S>(p, f_out, s);
+    default: return lbm::launch_stream_only<LBM_STORE_BF16S>(p, f_out, s);
+  }
+}
+
+static int convert(LbmPlan* pl, const float* in, float* out, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "plan not bound");
+  FusedParams p = params_for(pl);
+  cudaStream_t s = (cudaStream_t)stream;
+  void* cur = pl->parity ? pl->b.fb : pl->b.fa;
+  if (pl->d.storage == LBM_STORE_F32) {
+    const size_t bytes = 9 * p.plane * sizeof(float);
+    if (in && in != cur) return lbm_err::cuda(cudaMemcpyAsync(cur, in, bytes, cudaMemcpyDeviceToDevice, s), "import");
+    if (out && out != cur) return lbm_err::cuda(cudaMemcpyAsync(out, cur, bytes, cudaMemcpyDeviceToDevice, s), "export");
+    return LBM_OK;
+  }
+  if (pl->d.storage == LBM_STORE_F16S)
+    return in ? lbm::launch_convert<LBM_STORE_F16S>(p, in, cur, 1, s)
+              : lbm::launch_convert<LBM_STORE_F16S>(p, nullptr, out, 0, s);
+  return in ? lbm::launch_convert<LBM_STORE_BF16S>(p, in, cur, 1, s)
+            : lbm::launch_convert<LBM_STORE_BF16S>(p, nullptr, out, 0, s);
+}
+
+int lbm_plan_import(LbmPlan* pl, const float* f_post, void* stream) {
+  if (!f_post) return lbm_err::set(LBM_ERR_ARG, "plan_import: NULL source");
+  return convert(pl, f_post, nullptr, stream);
+}
+
+int lbm_plan_export(LbmPlan* pl, float* f_post, void* stream) {
+  if (!f_post) return lbm_err::set(LBM_ERR_ARG, "plan_export: NULL destination");
+  return convert(pl, nullptr, f_post, stream);
+}
+
+int lbm_plan_destroy(LbmPlan* pl) {
+  delete pl;
+  return LBM_OK;
+}
+
+int64_t lbm_reduce_scratch_doubles(void) { return (int64_t)lbm::REDUCE_BLOCKS * 3; }
+
+int lbm_plan_reduce_moments(LbmPlan* pl, double* partials, double* out, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "reduce: plan not bound");
+  if (!partials || !out) return lbm_err::set(LBM_ERR_ARG, "reduce: NULL scratch or output");
+  FusedParams p = params_for(pl);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return lbm::launch_reduce<LBM_STORE_F32>(p, partials, out, s);
+    case LBM_STORE_F16S: return lbm::launch_reduce<LBM_STORE_F16S>(p, partials, out, s);
+    default: return lbm::launch_reduce<LBM_STORE_BF16S>(p, partials, out, s);
+  }
+}
+
+}  // extern "C"

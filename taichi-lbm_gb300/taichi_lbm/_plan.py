@@ -1,0 +1,271 @@
+"""Compile a reference step composition into the fused kernel's node codes.
+
+Pure host logic (numpy), no CUDA.  Input: the lattice size, the collision
+group, the neighbor table in bit form and the ordered boundary list of a
+BoundaryEngine (taichi_lbm/BoundaryCondition.py:477-483 applies them in
+insertion order).  Output: one uint16 code per node (bounce bits, collide
+flag, saved-moments flag, boundary program id), the per-segment fast-path
+flags, the merged boundary instances and programs, and per-node boundary
+velocities.
+
+Semantics reproduced (reference step: moments, collision into f2, then every
+boundary in order, each reading and writing f and the moment fields):
+
+* A stream carrier (PeriodicAllBoundary, InsideBoundary, BounceBackWall)
+  rewrites all nine populations of its nodes from f2, so a node's last
+  carrier alone defines its post-stream populations: periodic -> pull with
+  wrap-around, bounce-back -> pull where neighbor != -1 else f2[x][opp k],
+  inside -> pull (a missing link is an out-of-range read in the reference and
+  is refused).
+* Rewrite boundaries that follow the node's last carrier are applied in
+  order as the node's program.
+* A boundary that reads f or moments of another node (NEEM, ABC, open
+  boundaries) reads the start-of-step moments and the post-stream
+  populations; compositions where an earlier boundary in the same step has
+  already modified those values are refused, as are reads outside the
+  lattice.
+
+Anything refused raises UnsupportedComposition with the reason; the caller
+can still run the same composition through the per-stage kernels.
+"""
+import numpy as np
+
+from . import _capi as A
+
+MOMENT_WRITERS = {A.BC_VELOCITY_EQ, A.BC_VELOCITY_NEEM, A.BC_PRESSURE_ABC, A.BC_PRESSURE_NEEM,
+                  A.BC_OPEN_NEUMANN, A.BC_OPEN_CONV1}
+# boundary kind -> (reads moments at self, reads moments at x2, reads f at x2, reads f at x3)
+READS = {
+    A.BC_VELOCITY_BB: (True, False, False, False),
+    A.BC_VELOCITY_EQ: (False, False, False, False),
+    A.BC_VELOCITY_NEEM: (False, True, True, False),
+    A.BC_PRESSURE_ABC: (True, True, False, False),
+    A.BC_PRESSURE_NEEM: (True, True, True, False),
+    A.BC_OPEN_NEUMANN: (False, False, True, False),
+    A.BC_OPEN_CONV1: (False, True, True, False),
+    A.BC_OPEN_EXTRAP: (False, False, True, True),
+}
+VELOCITY_KINDS = {A.BC_VELOCITY_BB, A.BC_VELOCITY_EQ, A.BC_VELOCITY_NEEM}
+CX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+CY = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+
+
+class UnsupportedComposition(ValueError):
+    """The fused kernel cannot reproduce this step composition exactly."""
+
+
+class BoundaryItem:
+    """One boundary of the ordered list, in plain data."""
+
+    def __init__(self, kind, nodes, direction=0, rho_value=0.0, velocity=None, name=""):
+        self.kind = int(kind)
+        self.nodes = np.asarray(nodes, np.int32).reshape(-1, 2)
+        self.direction = int(direction or 0)
+        self.rho_value = float(rho_value or 0.0)
+        self.velocity = None if velocity is None else np.asarray(velocity, np.float32).reshape(-1, 2)
+        self.name = name
+
+
+class CompiledPlan:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def _members(nx, ny, nodes):
+    m = np.zeros((nx, ny), bool)
+    if nodes.size:
+        m[nodes[:, 0], nodes[:, 1]] = True
+    return m
+
+
+def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
+    """links: (nx, ny) int array, LBField.neighbor in bit form (bit k: link k
+    has a source; bit 15: node classified)."""
+    V = int(nodes_per_thread)
+    active = _members(nx, ny, np.asarray(collision_nodes, np.int32).reshape(-1, 2))
+    carrier = np.full((nx, ny), -1, np.int32)
+    carrier_kind = np.zeros((nx, ny), np.int32)
+    covered = np.zeros((nx, ny), bool)
+    rewrites = []
+    for idx, it in enumerate(items):
+        nd = it.nodes
+        if nd.size and ((nd[:, 0] < 0).any() or (nd[:, 0] >= nx).any() or (nd[:, 1] < 0).any()
+                        or (nd[:, 1] >= ny).any()):
+            raise UnsupportedComposition(f"boundary '{it.name}' has nodes outside the lattice")
+        if it.kind == A.BC_FLUID:
+            continue
+        covered[nd[:, 0], nd[:, 1]] = True
+        if it.kind in (A.BC_PERIODIC, A.BC_INSIDE, A.BC_BOUNCEBACK):
+            carrier[nd[:, 0], nd[:, 1]] = idx
+            carrier_kind[nd[:, 0], nd[:, 1]] = it.kind
+        elif it.kind in READS:
+            rewrites.append(idx)
+        else:
+            raise UnsupportedComposition(f"boundary '{it.name}' (kind {it.kind}) has no fused form")
+
+    if (active & (carrier < 0)).any():
+        i, j = np.argwhere(active & (carrier < 0))[0]
+        raise UnsupportedComposition(f"colliding node ({i}, {j}) is not covered by any stream "
+                                     "carrier (its populations would not be streamed)")
+    if (covered & ~active).any():
+        i, j = np.argwhere(covered & ~active)[0]
+        raise UnsupportedComposition(f"node ({i}, {j}) is in a boundary group but not in the "
+                                     "collision group")
+
+    # --- bounce bits from each node's last carrier
+    code = np.zeros((nx, ny), np.int64)
+    code[active] |= A.CODE_ACTIVE
+    links = np.asarray(links, np.int64)
+    bb = active & (carrier_kind == A.BC_BOUNCEBACK)
+    ins = active & (carrier_kind == A.BC_INSIDE)
+    if ((bb | ins) & ((links & 0x8000) == 0)).any():
+        i, j = np.argwhere((bb | ins) & ((links & 0x8000) == 0))[0]
+        raise UnsupportedComposition(f"node ({i}, {j}) streams through the neighbor table but "
+                                     "was never classified (call neighbor_classify after the mask)")
+    for k in range(1, 9):
+        missing = ((links >> k) & 1) == 0
+        if (ins & missing).any():
+            i, j = np.argwhere(ins & missing)[0]
+            raise UnsupportedComposition(f"InsideBoundary node ({i}, {j}) has no source on link "
+                                         f"{k}: the reference reads outside the lattice there")
+        code[bb & missing] |= 1 << (k - 1)
+
+    # --- rewrite boundaries: ordering checks, reads, saves
+    member = {idx: _members(nx, ny, items[idx].nodes) for idx in rewrites}
+    f_modified_before = np.zeros((nx, ny), bool)
+    mom_modified_before = np.zeros((nx, ny), bool)
+    save = np.zeros((nx, ny), bool)
+    for idx in rewrites:
+        it = items[idx]
+        nd = it.nodes
+        if nd.size == 0:
+            continue
+        if (carrier[nd[:, 0], nd[:, 1]] > idx).any():
+            raise UnsupportedComposition(f"boundary '{it.name}' is applied before a stream carrier "
+                                         "that overwrites its nodes")
+        if it.direction not in (1, 2, 3, 4):
+            raise UnsupportedComposition(f"boundary '{it.name}' needs direction 1..4")
+        self_m, x2_m, x2_f, x3_f = READS[it.kind]
+        dx, dy = CX[it.direction], CY[it.direction]
+        x2 = nd - np.array([dx, dy], np.int32)
+        x3 = nd - 2 * np.array([dx, dy], np.int32)
+        for name, pts, need in (("x2", x2, x2_m or x2_f), ("x3", x3, x3_f)):
+            if not need:
+                continue
+            if ((pts[:, 0] < 0) | (pts[:, 0] >= nx) | (pts[:, 1] < 0) | (pts[:, 1] >= ny)).any():
+                raise UnsupportedComposition(f"boundary '{it.name}' reads a neighbour outside the lattice")
+            if not active[pts[:, 0], pts[:, 1]].all():
+                raise UnsupportedComposition(f"boundary '{it.name}' reads a non-colliding neighbour")
+            if member[idx][pts[:, 0], pts[:, 1]].any():
+                raise UnsupportedComposition(f"boundary '{it.name}' reads nodes of its own group "
+                                             "(order-dependent in the reference)")
+            if f_modified_before[pts[:, 0], pts[:, 1]].any() and (x2_f or x3_f):
+                raise UnsupportedComposition(f"boundary '{it.name}' reads populations an earlier "
+                                             "boundary already rewrote in the same step")
+        if x2_m:
+            if mom_modified_before[x2[:, 0], x2[:, 1]].any():
+                raise UnsupportedComposition(f"boundary '{it.name}' reads moments an earlier "
+                                             "boundary already rewrote in the same step")
+            save[x2[:, 0], x2[:, 1]] = True
+        if self_m:
+            if mom_modified_before[nd[:, 0], nd[:, 1]].any():
+                raise UnsupportedComposition(f"boundary '{it.name}' reads moments an earlier "
+                                             "boundary already rewrote in the same step")
+            save[nd[:, 0], nd[:, 1]] = True
+        f_modified_before |= member[idx]
+        if it.kind in MOMENT_WRITERS:
+            mom_modified_before |= member[idx]
+
+    # --- merge consecutive same-kind boundaries with disjoint groups
+    instances = []  # dicts: kind, direction, rho_value, members (list of idx)
+    for idx in rewrites:
+        it = items[idx]
+        if it.nodes.size == 0:
+            continue
+        last = instances[-1] if instances else None
+        if (last is not None and last["kind"] == it.kind and last["direction"] == it.direction
+                and last["rho_value"] == it.rho_value and last["last_idx"] == _prev_rewrite(rewrites, idx)
+                and not (last["mask"] & member[idx]).any()):
+            last["members"].append(idx)
+            last["mask"] |= member[idx]
+            last["last_idx"] = idx
+        else:
+            instances.append({"kind": it.kind, "direction": it.direction, "rho_value": it.rho_value,
+                              "members": [idx], "mask": member[idx].copy(), "last_idx": idx})
+    if len(instances) > A.MAX_BC:
+        raise UnsupportedComposition(f"{len(instances)} distinct rewrite boundaries "
+                                     f"(at most {A.MAX_BC} in one fused plan)")
+    inst_of_item = {}
+    for n, ins_ in enumerate(instances):
+        for idx in ins_["members"]:
+            inst_of_item[idx] = n
+
+    # per-node velocity planes (one velocity boundary per node)
+    bc_vel = None
+    vel_owner = np.full((nx, ny), -1, np.int32)
+    for idx in rewrites:
+        it = items[idx]
+        if it.kind not in VELOCITY_KINDS or it.nodes.size == 0:
+            continue
+        if bc_vel is None:
+            bc_vel = np.zeros((2, nx, ny), np.float32)
+        nd = it.nodes
+        v = it.velocity if it.velocity is not None else np.zeros((nd.shape[0], 2), np.float32)
+        clash = vel_owner[nd[:, 0], nd[:, 1]] >= 0
+        if clash.any():
+            old = bc_vel[:, nd[clash, 0], nd[clash, 1]].T
+            if not np.array_equal(old, v[clash]):
+                raise UnsupportedComposition("a node has two velocity boundaries with different values")
+        bc_vel[0, nd[:, 0], nd[:, 1]] = v[:, 0]
+        bc_vel[1, nd[:, 0], nd[:, 1]] = v[:, 1]
+        vel_owner[nd[:, 0], nd[:, 1]] = idx
+
+    # programs: ordered instance list per node
+    seqs = {}
+    node_prog = np.zeros((nx, ny), np.int64)
+    if rewrites:
+        lists = {}
+        for idx in rewrites:
+            nd = items[idx].nodes
+            n = inst_of_item.get(idx)
+            if n is None:
+                continue
+            for i, j in nd:
+                lst = lists.setdefault((int(i), int(j)), [])
+                if not lst or lst[-1] != n:
+                    lst.append(n)
+        for (i, j), lst in lists.items():
+            t = tuple(lst)
+            if len(t) > A.PROG_LEN:
+                raise UnsupportedComposition(f"node ({i}, {j}) has {len(t)} rewrite boundaries "
+                                             f"(at most {A.PROG_LEN})")
+            if t not in seqs:
+                seqs[t] = len(seqs) + 1
+            node_prog[i, j] = seqs[t]
+        if len(seqs) + 1 > A.MAX_PROG:
+            raise UnsupportedComposition(f"{len(seqs)} distinct boundary programs "
+                                         f"(at most {A.MAX_PROG - 1})")
+    code |= node_prog << A.CODE_PROG_SHIFT
+    code[save & active] |= A.CODE_SAVE
+
+    programs = np.full((A.MAX_PROG, A.PROG_LEN), -1, np.int8)
+    for t, pid in seqs.items():
+        programs[pid, :len(t)] = t
+
+    # --- segment flags: 0 when every node of the segment is plain
+    seg_w = 32 * V
+    nseg = (nx + seg_w - 1) // seg_w
+    plain = code == A.CODE_ACTIVE  # (nx, ny)
+    pad = nseg * seg_w - nx
+    notplain = np.pad(~plain, ((0, pad), (0, 0)), constant_values=False)
+    seg_flags = notplain.reshape(nseg, seg_w, ny).any(axis=1).T.astype(np.uint8)  # (ny, nseg)
+
+    return CompiledPlan(code=code.astype(np.uint16), seg_flags=np.ascontiguousarray(seg_flags),
+                        nseg=nseg, instances=instances, programs=programs, nprog=len(seqs) + 1,
+                        bc_vel=bc_vel, items=items, active=active, save=save,
+                        n_special_segments=int(seg_flags.sum()))
+
+
+def _prev_rewrite(rewrites, idx):
+    pos = rewrites.index(idx)
+    return rewrites[pos - 1] if pos > 0 else None

@@ -1,0 +1,222 @@
+"""Shan-Chen pseudopotential model: equations of state (taichi_lbm/EOS.py),
+the single-component force (taichi_lbm/ExternalForce.py) and psi boundaries
+(taichi_lbm/SCBoundaryCondition.py)."""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from .boundary import BoundaryCondition, PlaneBoundary
+from .fields import Field
+from .lbm import WEIGHTS, C, stream_handle
+
+
+class Pseudopotential:
+    """EOS.py:5-38.  Like the reference, rho_cr, pressure_cr and
+    temperature_cr are required keys."""
+
+    kind = None
+
+    def __init__(self, params):
+        p = {"a": None, "b": None, "R": 1.0, "G": 1.0}
+        p.update(params)
+        self.a, self.b, self.R, self.G = p["a"], p["b"], p["R"], p["G"]
+        self.rho_cr = params["rho_cr"]
+        self.pressure_cr = params["pressure_cr"]
+        self.temperature_cr = params["temperature_cr"]
+        self.omega = params.get("omega", 0.0)
+
+    def EOS(self, dens, T):
+        raise NotImplementedError
+
+    def get_psi(self, dens, T):
+        """Host evaluation in float32 (EOS.py:28-32)."""
+        dens = np.asarray(dens, np.float32)
+        T = np.asarray(T, np.float32)
+        p = self.EOS(dens, T)
+        return np.sqrt(np.abs(np.float32(6.0 / self.G) * (p - dens / np.float32(3.0))))
+
+    def struct(self):
+        e = _capi.LbmEos()
+        e.kind = self.kind
+        e.a, e.b = float(self.a or 0.0), float(self.b or 0.0)
+        e.R, e.G = float(self.R), float(self.G)
+        e.rho0 = 0.0
+        e.omega = float(self.omega or 0.0)
+        e.T_cr = float(self.temperature_cr or 1.0)
+        return e
+
+
+class SC_psi:
+    """EOS.py:40-47"""
+
+    kind = _capi.EOS_SC
+
+    def __init__(self, rho0):
+        self.rho0 = rho0
+
+    def get_psi(self, dens, T):
+        d = np.asarray(dens, np.float32)
+        r0 = np.float32(self.rho0)
+        return r0 * (np.float32(1) - np.exp(-d / r0))
+
+    def struct(self):
+        e = _capi.LbmEos()
+        e.kind = self.kind
+        e.rho0 = float(self.rho0)
+        e.R = e.G = 1.0
+        e.T_cr = 1.0
+        return e
+
+
+class vdW_psi(Pseudopotential):
+    """EOS.py:50-58"""
+    kind = _capi.EOS_VDW
+
+    def EOS(self, dens, T):
+        return dens * np.float32(self.R) * T / (1 - np.float32(self.b) * dens) - np.float32(self.a) * dens ** 2
+
+
+class RK_psi(Pseudopotential):
+    """EOS.py:61-69"""
+    kind = _capi.EOS_RK
+
+    def EOS(self, dens, T):
+        a, b, R = (np.float32(v) for v in (self.a, self.b, self.R))
+        return dens * R * T / (1 - b * dens) - a * dens ** 2 / np.sqrt(T) / (1 + b * dens)
+
+
+class PR_psi(Pseudopotential):
+    """EOS.py:72-82"""
+    kind = _capi.EOS_PR
+
+    def __init__(self, params):
+        super().__init__(params)
+        self.omega = params["omega"]
+
+    def EOS(self, dens, T):
+        a, b, R = (np.float32(v) for v in (self.a, self.b, self.R))
+        om = self.omega
+        kap = np.float32(0.37464 + 1.54226 * om - 0.269922 * om * om)
+        alpha = (1 + kap * (1 - np.sqrt(T / np.float32(self.temperature_cr)))) ** 2
+        return dens * R * T / (1 - b * dens) - a * alpha * dens ** 2 / (1 + 2 * b * dens - (b * dens) ** 2)
+
+
+class CS_psi(Pseudopotential):
+    """EOS.py:85-95 (Carnahan-Starling)"""
+    kind = _capi.EOS_CS
+
+    def EOS(self, dens, T):
+        a, b, R = (np.float32(v) for v in (self.a, self.b, self.R))
+        b4 = b * dens / 4
+        return dens * R * T * (1 + b4 + b4 ** 2 - b4 ** 3) / (1 - b4) ** 3 - a * dens ** 2
+
+
+class ShanChenModel:
+    """ExternalForce.py:5-27: psi on a one-node halo around the lattice."""
+
+    def __init__(self, lb_field, group):
+        self.group = group
+        self.wc = (WEIGHTS[:, None] * C).astype(np.float32)
+        self.psi_field = Field(lb_field, "_psi", lb_field.NX, lb_field.NY, "sc", halo=1)
+
+
+class ShanChenForceC1(ShanChenModel):
+    """ExternalForce.py:122-158: single-component Shan-Chen force."""
+
+    def __init__(self, params):
+        p = {"lb_field": None, "g_coh": None, "group": None, "psi": None}
+        p.update(params)
+        super().__init__(p["lb_field"], p["group"])
+        self.g_coh = p["g_coh"]
+        self.psi = p["psi"]
+
+    def update_psi(self, lb_field):
+        lb_field._sync_fused()
+        L = lb_field._lattice()
+        e = self.psi.struct()
+        _capi.call("lbm_sc_update_psi", ctypes.byref(L), ctypes.byref(e), self.group.ptr,
+                   self.group.n, stream_handle())
+
+    def cau_SCforce(self, lb_field):
+        lb_field._sync_fused()
+        L = lb_field._lattice()
+        _capi.call("lbm_sc_force", ctypes.byref(L), float(self.g_coh), self.group.ptr,
+                   self.group.n, stream_handle())
+
+
+class ShanChenForceC2(ShanChenModel):
+    """ExternalForce.py:161-212 (two components) — not part of this build."""
+
+    def __init__(self, params):
+        raise NotImplementedError("two-component Shan-Chen (ShanChenForceC2) is not built; "
+                                  "this build runs single-component lattices")
+
+
+# ------------------------------------------------------------ psi boundaries
+class PeriodicPsi_LR:
+    """SCBoundaryCondition.py:365-373"""
+
+    def apply(self, lb_field):
+        L = lb_field._lattice()
+        _capi.call("lbm_psi_periodic", ctypes.byref(L), 0, stream_handle())
+
+
+class PeriodicPsi_BT:
+    """SCBoundaryCondition.py:375-383"""
+
+    def apply(self, lb_field):
+        L = lb_field._lattice()
+        _capi.call("lbm_psi_periodic", ctypes.byref(L), 1, stream_handle())
+
+
+class FixedPsi(BoundaryCondition):
+    """SCBoundaryCondition.py:352-362"""
+
+    def __init__(self, spec, psi_value):
+        super().__init__(spec)
+        self.psi_value = psi_value
+
+    def apply(self, lb_field):
+        L = lb_field._lattice()
+        _capi.call("lbm_psi_fixed", ctypes.byref(L), self.group.ptr, self.group.n,
+                   float(self.psi_value), stream_handle())
+
+
+class OpenBoundaryPsi(PlaneBoundary):
+    """SCBoundaryCondition.py:9-16.  The open psi boundaries
+    (OpenNeumannPsi, OpenConvective1orderPsi, OpenConvective2orderPsi,
+    OpenExtrapolationPsi) have no CUDA kernel in this build."""
+
+    def apply(self, lb_field):
+        raise NotImplementedError(f"{type(self).__name__} has no CUDA kernel in this build")
+
+
+class OpenNeumannPsi(OpenBoundaryPsi):
+    pass
+
+
+class OpenConvective1orderPsi(OpenBoundaryPsi):
+    pass
+
+
+class OpenConvective2orderPsi(OpenBoundaryPsi):
+    pass
+
+
+class OpenExtrapolationPsi(OpenBoundaryPsi):
+    pass
+
+
+class BoundaryEngineSC:
+    """SCBoundaryCondition.py:388-399"""
+
+    def __init__(self):
+        self.boundary_conditions = {}
+
+    def add_boundary_condition(self, name, bc):
+        self.boundary_conditions[name] = bc
+
+    def apply_boundary_conditions(self, lb_field):
+        for bc in self.boundary_conditions.values():
+            bc.apply(lb_field)

@@ -1,0 +1,271 @@
+"""FusedSolver: the whole reference step as one CUDA kernel per time step.
+
+The reference leaves the step composition to the user's ``lbm_solve()``
+(cases/Circular cylinder.py:182-193, cases/Power Law Fluid.py:160-173):
+
+    density -> pressure -> force_density -> velocity
+    [-> shear_rate -> relaxation_time]   (power-law fluid)
+    -> collision.apply -> boundary_engine.apply_boundary_conditions
+
+``FusedSolver(lb_field, macroscopic_engine, collision, boundary_engine)``
+runs exactly that composition; ``step(n)`` equals n calls of that
+``lbm_solve()`` followed by the moment prologue of the next step (so ``rho``
+and ``vel`` hold the moments of the final ``f``).  Internally: the first
+collision runs through the per-stage kernels, then n-1 fused launches (each
+= boundary pass of step k-1 + moments/collision of step k), then one stream
+and boundary pass and the moment kernels.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi as A
+from ._plan import BoundaryItem, UnsupportedComposition, compile_plan
+from .boundary import BoundaryCondition
+from .collision import BGKCollision, MRTCollision, PowerLawFluid, TRTCollision
+from .lbm import stream_handle
+
+STORAGE = {"fp32": A.STORE_F32, "fp16s": A.STORE_F16S, "bf16s": A.STORE_BF16S}
+DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 8, A.STORE_BF16S: 8}
+
+
+def boundary_items(boundary_engine):
+    items = []
+    for name, bc in boundary_engine.boundary_conditions.items():
+        if not isinstance(bc, BoundaryCondition):
+            raise UnsupportedComposition(f"boundary '{name}' is not a BoundaryCondition")
+        vel = None
+        if hasattr(bc, "velocity_value"):
+            vel = bc.per_node_velocity_host()
+        items.append(BoundaryItem(bc.kind, bc.group.nodes, getattr(bc, "direction", 0),
+                                  getattr(bc, "rho_value", 0.0), vel, name))
+    return items
+
+
+class FusedSolver:
+    def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
+                 nodes_per_thread=None, local_relaxation=None):
+        if lb_field.sc_field is not None:
+            raise UnsupportedComposition("Shan-Chen lattices use the per-stage kernels in this build")
+        self.lb = lb_field
+        self.me = macroscopic_engine
+        self.coll = collision
+        self.be = boundary_engine
+        self.storage = STORAGE[storage] if isinstance(storage, str) else int(storage)
+        self.V = int(nodes_per_thread or DEFAULT_V[self.storage])
+        if local_relaxation is None:
+            local_relaxation = isinstance(collision.fluid_model, PowerLawFluid)
+        self.powerlaw = bool(local_relaxation)
+        if self.powerlaw and not isinstance(collision.fluid_model, PowerLawFluid):
+            raise UnsupportedComposition("local relaxation needs a PowerLawFluid")
+        if macroscopic_engine.group is not collision.group and not np.array_equal(
+                macroscopic_engine.group.nodes, collision.group.nodes):
+            raise UnsupportedComposition("the macroscopic and collision groups differ")
+        self.group = collision.group
+        self._plan = None
+        self._owns = False
+        self._build()
+
+    # ------------------------------------------------------------ build
+    def _uniform(self, field_tensor, planes=None):
+        nd = torch.as_tensor(self.group.nodes, device=field_tensor.device).long()
+        if planes is None:
+            v = field_tensor[nd[:, 1], nd[:, 0]]
+            vals = torch.unique(v)
+            if vals.numel() != 1:
+                raise UnsupportedComposition("per-node relaxation times differ across the group "
+                                             "(Newtonian fused path needs a uniform tau)")
+            return float(vals[0].item())
+        out = []
+        for a in planes:
+            vals = torch.unique(field_tensor[a][nd[:, 1], nd[:, 0]])
+            if vals.numel() != 1:
+                raise UnsupportedComposition(f"MRT rate s{a} differs across the group")
+            out.append(float(vals[0].item()))
+        return out
+
+    def _build(self):
+        lb, c = self.lb, self.coll
+        nx, ny, P = lb.NX, lb.NY, lb.pitch
+        cp = compile_plan(nx, ny, self.group.nodes, lb.links_host(), boundary_items(self.be), self.V)
+        self.compiled = cp
+        dev = lb.device
+        d = A.LbmPlanDesc()
+        d.nx, d.ny, d.pitch = nx, ny, P
+        d.storage = self.storage
+        d.nodes_per_thread = self.V
+        d.fluid_model = A.POWERLAW if self.powerlaw else A.NEWTONIAN
+        d.tau_min, d.tau_max = float(c.tau_min), float(c.tau_max)
+        if self.powerlaw:
+            d.pl_m, d.pl_n = float(c.fluid_model.m), float(c.fluid_model.n)
+        if isinstance(c, BGKCollision):
+            d.model = A.BGK
+            self.tau_state = c._tau
+            d.tau = 1.0 if self.powerlaw else self._uniform(c._tau)
+        elif isinstance(c, TRTCollision):
+            d.model = A.TRT
+            d.magic = float(c.magic[0])
+            self.tau_state = c._tau_sym
+            if not self.powerlaw:
+                d.tau = self._uniform(c._tau_sym)
+                d.tau_antisym = self._uniform(c._tau_antisym)
+            else:
+                d.tau = d.tau_antisym = 1.0
+        elif isinstance(c, MRTCollision):
+            d.model = A.MRT
+            self.tau_state = c._diag[7]
+            planes = [0, 1, 2, 3, 4, 5, 6] + ([] if self.powerlaw else [7, 8])
+            s = self._uniform(c._diag, planes)
+            for a, v in zip(planes, s):
+                d.mrt_s[a] = v
+            d.tau = 1.0
+            if self.powerlaw and not torch.equal(c._diag[7], c._diag[8]):
+                raise UnsupportedComposition("MRT power law needs diag[7] == diag[8]")
+        else:
+            raise UnsupportedComposition(f"unknown collision {type(c).__name__}")
+        g = np.asarray(lb.gravity_force, np.float32).reshape(2)
+        d.gravity[0], d.gravity[1] = float(g[0]), float(g[1])
+
+        # device-side plan data
+        self.code = torch.zeros((ny, P), dtype=torch.int16, device=dev)
+        self.code[:, :nx] = torch.as_tensor(cp.code.T.astype(np.int16), device=dev)
+        self.seg_flags = torch.as_tensor(cp.seg_flags, device=dev)
+        self.bc_vel = None
+        if cp.bc_vel is not None:
+            self.bc_vel = torch.zeros((2, ny, P), dtype=torch.float32, device=dev)
+            self.bc_vel[:, :, :nx] = torch.as_tensor(np.transpose(cp.bc_vel, (0, 2, 1)).copy(),
+                                                     device=dev)
+        d.nbc = len(cp.instances)
+        for n, ins in enumerate(cp.instances):
+            b = d.bc[n]
+            b.kind, b.direction, b.rho_value = ins["kind"], ins["direction"], ins["rho_value"]
+            b.velocity_per_node = (self.bc_vel.data_ptr()
+                                   if ins["kind"] in (A.BC_VELOCITY_BB, A.BC_VELOCITY_EQ,
+                                                      A.BC_VELOCITY_NEEM) else None)
+        d.nprog = cp.nprog
+        for p in range(A.MAX_PROG):
+            for s in range(A.PROG_LEN):
+                d.prog[p][s] = int(cp.programs[p, s])
+        self.desc = d
+        self.mom = [torch.zeros((3, ny, P), dtype=torch.float32, device=dev) for _ in range(2)]
+        if self.storage == A.STORE_F32:
+            self.fbuf = None
+        else:
+            self.fbuf = [torch.zeros((9, ny, P), dtype=torch.float16 if self.storage == A.STORE_F16S
+                                     else torch.bfloat16, device=dev) for _ in range(2)]
+        plan = ctypes.c_void_p()
+        A.call("lbm_plan_create", ctypes.byref(d), ctypes.byref(plan))
+        self._plan = plan
+        self.parity = 0
+
+    def __del__(self):
+        try:
+            if self._plan is not None:
+                A.load().lbm_plan_destroy(self._plan)
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ running
+    def _bind(self):
+        lb = self.lb
+        b = A.LbmPlanBuffers()
+        if self.fbuf is None:
+            b.fa, b.fb = lb._f2.data_ptr(), lb._f.data_ptr()
+        else:
+            b.fa, b.fb = self.fbuf[0].data_ptr(), self.fbuf[1].data_ptr()
+        b.mom_a, b.mom_b = self.mom[0].data_ptr(), self.mom[1].data_ptr()
+        b.code = self.code.data_ptr()
+        b.seg_flags = self.seg_flags.data_ptr()
+        b.bc_vel = None if self.bc_vel is None else self.bc_vel.data_ptr()
+        b.tau = self.tau_state.data_ptr() if self.powerlaw else None
+        A.call("lbm_plan_bind", self._plan, ctypes.byref(b))
+
+    def _staged_first_step(self):
+        lb, me, c = self.lb, self.me, self.coll
+        me.density(lb)
+        me.pressure(lb)
+        me.force_density(lb)
+        me.velocity(lb)
+        if self.powerlaw:
+            c.shear_rate(lb)
+            c.relaxation_time(lb)
+        c.apply(lb)
+
+    def begin(self):
+        """Run the first collision and load the fused state (f2, moments)."""
+        lb = self.lb
+        self._staged_first_step()
+        self._bind()
+        A.call("lbm_plan_set_parity", self._plan, 0)
+        self.mom[0][0].copy_(lb._rho)
+        self.mom[0][1:3].copy_(lb._vel)
+        if self.fbuf is not None:
+            A.call("lbm_plan_import", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), stream_handle())
+        lb._fused_owner = self
+        self._live = True
+
+    def run(self, nsteps):
+        """nsteps fused launches on the current state (no staging)."""
+        A.call("lbm_plan_run", self._plan, int(nsteps), stream_handle())
+
+    def finish(self):
+        """Last stream/boundary pass and moment prologue; f, f2, rho, vel current."""
+        lb = self.lb
+        lb._fused_owner = None
+        self._live = False
+        par = ctypes.c_int32()
+        A.call("lbm_plan_get_parity", self._plan, ctypes.byref(par))
+        s = stream_handle()
+        if self.fbuf is None:
+            if par.value == 0:  # state in f2 -> write f
+                A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
+            else:  # state in f's storage -> stream into f2's storage, then swap roles
+                A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
+                lb._f, lb._f2 = lb._f2, lb._f
+        else:
+            A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
+            A.call("lbm_plan_export", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
+        if self.powerlaw:
+            c = self.coll
+            nd = torch.as_tensor(self.group.nodes, device=lb.device).long()
+            if isinstance(c, TRTCollision):
+                ts = c._tau_sym[nd[:, 1], nd[:, 0]]
+                c._tau_antisym[nd[:, 1], nd[:, 0]] = float(c.magic[0]) / (ts - 0.5) + 0.5
+            elif isinstance(c, MRTCollision):
+                c._diag[8].copy_(c._diag[7])
+        me = self.me
+        me.density(lb)
+        me.pressure(lb)
+        me.force_density(lb)
+        me.velocity(lb)
+
+    def sync(self):
+        if getattr(self, "_live", False):
+            self.finish()
+
+    def parity_now(self):
+        """0: the live state is in the first buffer (f2's storage for fp32)."""
+        par = ctypes.c_int32()
+        A.call("lbm_plan_get_parity", self._plan, ctypes.byref(par))
+        return par.value
+
+    def step(self, n=1):
+        """n reference steps (n calls of lbm_solve()) + the next moment prologue."""
+        n = int(n)
+        if n <= 0:
+            return
+        self.begin()
+        if n > 1:
+            self.run(n - 1)
+        self.finish()
+
+    def reduce_moments(self):
+        """FP64 (sum f, sum f cx, sum f cy) over colliding nodes of the live
+        fused state (call between begin() and finish())."""
+        scratch = torch.empty(int(A.load().lbm_reduce_scratch_doubles()), dtype=torch.float64,
+                              device=self.lb.device)
+        out = torch.empty(3, dtype=torch.float64, device=self.lb.device)
+        A.call("lbm_plan_reduce_moments", self._plan, ctypes.c_void_p(scratch.data_ptr()),
+               ctypes.c_void_p(out.data_ptr()), stream_handle())
+        return out

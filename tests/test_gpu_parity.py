@@ -1,0 +1,169 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference-source
+fixtures and against the CPU oracle on identical inputs.
+
+Tolerance (fp32): max|a - b| / max|b| per field <= 1e-5 after N steps
+(velocity is compared the same way because u -> 0 at walls).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.cases import (build_from_case, cylinder_channel, describe, fields_of, fixture_names,
+                         load_fixture, rel_err, run_staged)
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+# power law: gamma^(n-1) amplifies last-bit differences of the strain rate
+TOL_PL = 5e-5
+F64_CASES = {n for n in fixture_names() if n.endswith("_f64")}
+SC_CASES = {n for n in fixture_names() if n.startswith("sc_")}
+
+
+@pytest.fixture(scope="module")
+def tl(built):
+    import taichi_lbm
+    return taichi_lbm
+
+
+def tol_for(meta):
+    return TOL_PL if meta["step_kind"] == "powerlaw" else TOL
+
+
+@pytest.mark.parametrize("name", sorted(set(fixture_names()) - F64_CASES))
+def test_staged_matches_reference_fixture(tl, name):
+    meta, arrays = load_fixture(name)
+    lb, me, coll, be, sc, bsc = build_from_case(tl, meta, arrays)
+    run_staged(lb, me, coll, be, sc, bsc, meta["step_kind"], meta["steps"])
+    torch.cuda.synchronize()
+    got = fields_of(lb)
+    tol = tol_for(meta)
+    for k in ("f", "f2", "rho", "vel", "pressure"):
+        assert rel_err(got[k], arrays[k]) < tol, (k, rel_err(got[k], arrays[k]))
+    if "psi" in got:
+        assert rel_err(got["psi"], arrays["psi"]) < tol
+
+
+@pytest.mark.parametrize("name", sorted(set(fixture_names()) - F64_CASES - SC_CASES))
+def test_fused_matches_reference_fixture(tl, name):
+    meta, arrays = load_fixture(name)
+    lb, me, coll, be, sc, bsc = build_from_case(tl, meta, arrays)
+    solver = tl.FusedSolver(lb, me, coll, be)
+    solver.step(meta["steps"])
+    torch.cuda.synchronize()
+    got = fields_of(lb)
+    tol = tol_for(meta)
+    for k in ("f", "f2", "rho", "vel"):
+        assert rel_err(got[k], arrays[k]) < tol, (k, rel_err(got[k], arrays[k]))
+
+
+def test_value_fn_inlet_equals_per_node_boundaries(tl):
+    """One VelocityEquilibrium with BoundarySpec.value_fn == the reference's
+    one-boundary-per-node parabolic inlet."""
+    meta, arrays = load_fixture("cyl_bgk_f32")
+    lb, me, coll, be, _, _ = build_from_case(tl, meta, arrays, value_fn_inlet=True)
+    assert sum(1 for n in be.boundary_conditions if n.startswith("inlet")) == 1
+    tl.FusedSolver(lb, me, coll, be).step(meta["steps"])
+    got = fields_of(lb)
+    for k in ("f", "rho", "vel"):
+        assert rel_err(got[k], arrays[k]) < TOL
+
+
+@pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
+@pytest.mark.parametrize("shape", [(256, 64), (301, 67)])
+def test_fused_matches_oracle_cylinder(tl, model, shape):
+    """Larger lattices (one odd width exercises the row-end wrap) against the
+    oracle: 200 steps."""
+    nx, ny = shape
+    s = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1 / 0.56, 1 / 0.56] if model == "mrt" else None
+    lb, me, coll, be = cylinder_channel(tl, nx, ny, ny / 10, nx / 5, ny / 2 - 0.5, 0.56, 0.05,
+                                        model=model, mrt_s=s)
+    meta, arrays = describe(lb, coll, be, 200)
+    tl.FusedSolver(lb, me, coll, be).step(200)
+    ref = O.replay(meta, arrays)
+    got = fields_of(lb)
+    for k in ("f", "rho", "vel"):
+        assert rel_err(got[k], ref[k]) < 2 * TOL, (k, rel_err(got[k], ref[k]))
+
+
+def test_fused_periodic_box_odd_width(tl):
+    """Fully periodic lattice whose width is not a multiple of the vector
+    width: every wrap-around path of the pull loads."""
+    nx, ny = 37, 23
+    lb = tl.LBField("box", nx, ny, 1)
+    lb.keep_init_snapshot = True
+    cls = tl.BoundaryClassifier((nx, ny))
+    be = tl.BoundaryEngine()
+    fl = tl.FluidBoundary(spec=tl.BoundarySpec(geometry_fn=lambda i, j: lb.mask[i, j] == 1))
+    fl.precompute(cls)
+    be.add_boundary_condition("fluid", fl)
+    per = tl.PeriodicAllBoundary(spec=tl.BoundarySpec(geometry_fn=lambda i, j: lb.mask[i, j] == 1))
+    per.precompute(cls)
+    be.add_boundary_condition("periodic", per)
+    lb.neighbor_classify()
+    me = tl.MacroscopicEngine(fl.group)
+    coll = tl.TRTCollision({"group": fl.group, "fluid_model": tl.NewtonianFluid(0.05), "NX": nx,
+                            "NY": ny, "num_components": 1, "shearviscosity": [0.05], "magic": [0.25]})
+    rng = np.random.default_rng(7)
+    lb.rho.from_numpy((1 + 0.02 * rng.random((nx, ny, 1))).astype(np.float32))
+    lb.vel.from_numpy((0.03 * (rng.random((nx, ny, 2)) - 0.5)).astype(np.float32))
+    lb.set_gravity([1e-5, -2e-5])
+    lb.init_LBM(coll, fl.group)
+    meta, arrays = describe(lb, coll, be, 150)
+    tl.FusedSolver(lb, me, coll, be).step(150)
+    ref = O.replay(meta, arrays)
+    got = fields_of(lb)
+    for k in ("f", "rho", "vel"):
+        assert rel_err(got[k], ref[k]) < 2 * TOL, (k, rel_err(got[k], ref[k]))
+
+
+def test_fused_equals_staged_and_run_is_resumable(tl):
+    """step(30) == step(10) three times == 30 staged steps."""
+    runs = []
+    for mode in ("one", "three", "staged"):
+        lb, me, coll, be = cylinder_channel(tl, 160, 48, 4.8, 32.0, 23.5, 0.6, 0.05, model="trt")
+        if mode == "one":
+            tl.FusedSolver(lb, me, coll, be).step(30)
+        elif mode == "three":
+            s = tl.FusedSolver(lb, me, coll, be)
+            for _ in range(3):
+                s.step(10)
+        else:
+            run_staged(lb, me, coll, be, None, None, "standard", 30)
+        runs.append(fields_of(lb))
+    for k in ("f", "f2", "rho", "vel"):
+        assert rel_err(runs[0][k], runs[2][k]) < TOL, k
+        assert rel_err(runs[1][k], runs[2][k]) < TOL, k
+
+
+@pytest.mark.parametrize("storage,tol", [("fp16s", 2e-3), ("bf16s", 2e-2)])
+def test_shifted_storage_against_fp64_oracle(tl, storage, tol):
+    nx, ny = 256, 64
+    lb, me, coll, be = cylinder_channel(tl, nx, ny, 6.4, 51.2, 31.5, 0.6, 0.04, model="bgk")
+    meta, arrays = describe(lb, coll, be, 300)
+    meta["fp"] = "f64"
+    tl.FusedSolver(lb, me, coll, be, storage=storage).step(300)
+    ref = O.replay(meta, arrays)
+    got = fields_of(lb)
+    assert rel_err(got["rho"], ref["rho"]) < tol
+    assert rel_err(got["vel"], ref["vel"]) < 10 * tol
+
+
+def test_fp64_mass_reduction(tl):
+    nx, ny = 200, 50
+    lb, me, coll, be = cylinder_channel(tl, nx, ny, 5.0, 40.0, 24.5, 0.6, 0.04)
+    s = tl.FusedSolver(lb, me, coll, be)
+    s.begin()
+    s.run(5)
+    out = s.reduce_moments().cpu().numpy()
+    par = s.parity_now()
+    state = (lb._f2 if par == 0 else lb._f)[:, :, :nx].double()
+    nd = torch.as_tensor(coll.group.nodes, device=state.device).long()
+    sel = state[:, nd[:, 1], nd[:, 0]]
+    c = torch.tensor([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]],
+                     dtype=torch.float64, device=state.device)
+    exp = [sel.sum().item(), (sel * c[:, 0:1]).sum().item(), (sel * c[:, 1:2]).sum().item()]
+    s.finish()
+    assert abs(out[0] - exp[0]) / exp[0] < 1e-12
+    assert abs(out[1] - exp[1]) < 1e-9 and abs(out[2] - exp[2]) < 1e-9

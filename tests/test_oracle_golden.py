@@ -1,0 +1,52 @@
+"""The CPU oracle against fixtures produced by the reference's own source
+(tests/golden/make_golden.py).  Float results are bit-identical except where
+the fixture used numpy's exp/pow and the oracle uses libm's."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.cases import fixture_names, load_fixture, rel_err
+
+# cases whose arithmetic goes through exp() or pow(x, 2.0): numpy and libm
+# may differ in the last bit there
+LIBM_TOL = {"sc_scpsi_mrt_f32": 1e-4, "sc_vdw_trt_f64": 1e-9}
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_oracle_reproduces_reference_fixture(name, built):
+    meta, arrays = load_fixture(name)
+    out = O.replay(meta, arrays)
+    assert out["error"] == 0
+    assert np.array_equal(out["mask"], arrays["mask"])
+    assert np.array_equal(out["neighbor"], arrays["neighbor"])
+    tol = LIBM_TOL.get(name)
+    for k in ("f", "f2", "rho", "vel", "pressure", "shear_rate"):
+        if tol is None:
+            assert np.array_equal(out[k], arrays[k]), f"{k} not bit-identical"
+        else:
+            assert rel_err(out[k], arrays[k]) < tol, k
+    if "psi" in arrays:
+        assert rel_err(out["psi"], arrays["psi"]) < (tol or 0.0) + 1e-30 or np.array_equal(out["psi"], arrays["psi"])
+
+
+@pytest.mark.parametrize("name", ["cyl_bgk_f32", "chan_inside_eq_bgk_f32", "contraction_pl_trt_n05_f32"])
+def test_oracle_mask_helpers_match_fixture(name, built):
+    meta, arrays = load_fixture(name)
+    o = O.Oracle(meta["NX"], meta["NY"], meta["fp"] == "f64")
+    if meta.get("disc"):
+        o.L.orc_mask_circle(o.h, *meta["disc"])
+    for r in meta.get("rects", []):
+        o.L.orc_mask_rect(o.h, *r)
+    assert np.array_equal(o.field("mask"), arrays["mask"])
+
+
+def test_fixture_groups_are_consistent(built):
+    """Every fixture's groups are inside the lattice and within the fluid."""
+    for name in fixture_names():
+        meta, arrays = load_fixture(name)
+        fluid = arrays["g_" + meta["bcs"][0]["name"]]
+        fl = set(map(tuple, fluid))
+        for b in meta["bcs"]:
+            g = arrays["g_" + b["name"]]
+            assert g.shape[1] == 2
+            assert set(map(tuple, g)) <= fl, (name, b["name"])
