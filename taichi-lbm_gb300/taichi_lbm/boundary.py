@@ -23,6 +23,7 @@ class MaskAndGroup:
     def __init__(self, nodes, device):
         nodes = np.ascontiguousarray(np.asarray(nodes, np.int32).reshape(-1, 2))
         self.nodes = nodes
+        self._checked = set()
         self.count = _Count(nodes.shape[0])
         self.group = torch.as_tensor(nodes if nodes.size else np.zeros((1, 2), np.int32),
                                      device=device)
@@ -34,6 +35,25 @@ class MaskAndGroup:
     @property
     def ptr(self):
         return ctypes.c_void_p(self.group.data_ptr())
+
+    def on(self, lattice, halo=0):
+        """Validate against a lattice (anything with NX, NY; halo=1 admits the
+        psi ring) and return self."""
+        self.require_inside(lattice.NX + 2 * halo, lattice.NY + 2 * halo, (-halo, -halo))
+        return self
+
+    def require_inside(self, nx, ny, shift=(0, 0), what="group"):
+        """Raise unless every node (minus shift) lies in the lattice: the
+        kernels index fields with these coordinates."""
+        key = (nx, ny, tuple(shift))
+        if key in self._checked:
+            return
+        nd = self.nodes - np.asarray(shift, np.int32)
+        if nd.size and ((nd[:, 0] < 0).any() or (nd[:, 0] >= nx).any() or (nd[:, 1] < 0).any()
+                        or (nd[:, 1] >= ny).any()):
+            raise ValueError(f"{what} has nodes whose {'neighbour ' if any(shift) else ''}"
+                             f"coordinates fall outside the {nx} x {ny} lattice")
+        self._checked.add(key)
 
 
 class _Count:
@@ -178,9 +198,25 @@ class BoundaryCondition:
             return np.tile(self.velocity_array(), (self.group.n, 1))
         return evaluate_values(fn, self.group.nodes)
 
+    # kinds that read the neighbour x - c_dir (1) or also x - 2 c_dir (2)
+    NEIGHBOUR_DEPTH = {_capi.BC_VELOCITY_NEEM: 1, _capi.BC_PRESSURE_ABC: 1,
+                       _capi.BC_PRESSURE_NEEM: 1, _capi.BC_OPEN_NEUMANN: 1, _capi.BC_OPEN_CONV1: 1,
+                       _capi.BC_OPEN_CONV2: 2, _capi.BC_OPEN_EXTRAP: 2}
+
+    def check(self, lb_field):
+        g = self.group
+        g.require_inside(lb_field.NX, lb_field.NY, what=type(self).__name__)
+        depth = self.NEIGHBOUR_DEPTH.get(self.kind, 0)
+        if depth:
+            c = lb_field.c[self.direction]
+            for d in range(1, depth + 1):
+                g.require_inside(lb_field.NX, lb_field.NY, (d * int(c[0]), d * int(c[1])),
+                                 what=type(self).__name__)
+
     def apply(self, lb_field):
         if self.kind == _capi.BC_FLUID:
             return
+        self.check(lb_field)
         lb_field._sync_fused()
         L = lb_field._lattice()
         b = self._struct(lb_field)

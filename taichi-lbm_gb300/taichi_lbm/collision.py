@@ -130,14 +130,14 @@ class Collision:
         lb_field._sync_fused()
         L = lb_field._lattice()
         c = self._init_struct() if init else self._struct()
-        _capi.call(fn, ctypes.byref(L), ctypes.byref(c), self.group.ptr, self.group.n,
+        _capi.call(fn, ctypes.byref(L), ctypes.byref(c), self.group.on(lb_field).ptr, self.group.n,
                    stream_handle())
 
     def initTau(self, lb_field=None):
         c = self._init_struct()
         L = _capi.LbmLattice()
         L.nx, L.ny, L.pitch = self.NX, self.NY, self.pitch
-        _capi.call("lbm_collision_init_tau", ctypes.byref(L), ctypes.byref(c), self.group.ptr,
+        _capi.call("lbm_collision_init_tau", ctypes.byref(L), ctypes.byref(c), self.group.on(self).ptr,
                    self.group.n, stream_handle())
 
     def shear_rate(self, lb_field):

@@ -184,7 +184,7 @@ class LBField:
             self._init_snapshot = (self.rho.to_numpy()[:, :, 0].copy(), self.vel.to_numpy().copy(),
                                    self.T.to_numpy().copy())
         L = self._lattice()
-        _capi.call("lbm_init_feq", ctypes.byref(L), group.ptr, group.n, stream_handle())
+        _capi.call("lbm_init_feq", ctypes.byref(L), group.on(self).ptr, group.n, stream_handle())
 
     def neighbor_classify(self):
         """Pull-source table from the mask (lbm.py:127-142)."""
@@ -207,13 +207,13 @@ class MacroscopicEngine:
     def density(self, lb_field):
         lb_field._sync_fused()
         L = lb_field._lattice()
-        _capi.call("lbm_density", ctypes.byref(L), self.group.ptr, self.group.n, stream_handle())
+        _capi.call("lbm_density", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n, stream_handle())
 
     def pressure(self, lb_field):
         lb_field._sync_fused()
         L = lb_field._lattice()
         sc = lb_field.sc_field
-        _capi.call("lbm_pressure", ctypes.byref(L), self.group.ptr, self.group.n,
+        _capi.call("lbm_pressure", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n,
                    0 if sc is None else 1, 0.0 if sc is None else float(sc.g_coh), stream_handle())
 
     pressure0 = pressure
@@ -222,10 +222,10 @@ class MacroscopicEngine:
     def force_density(self, lb_field):
         lb_field._sync_fused()
         L = lb_field._lattice()
-        _capi.call("lbm_force_density", ctypes.byref(L), self.group.ptr, self.group.n,
+        _capi.call("lbm_force_density", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n,
                    stream_handle())
 
     def velocity(self, lb_field):
         lb_field._sync_fused()
         L = lb_field._lattice()
-        _capi.call("lbm_velocity", ctypes.byref(L), self.group.ptr, self.group.n, stream_handle())
+        _capi.call("lbm_velocity", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n, stream_handle())

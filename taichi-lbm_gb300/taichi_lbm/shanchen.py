@@ -135,13 +135,13 @@ class ShanChenForceC1(ShanChenModel):
         lb_field._sync_fused()
         L = lb_field._lattice()
         e = self.psi.struct()
-        _capi.call("lbm_sc_update_psi", ctypes.byref(L), ctypes.byref(e), self.group.ptr,
+        _capi.call("lbm_sc_update_psi", ctypes.byref(L), ctypes.byref(e), self.group.on(lb_field).ptr,
                    self.group.n, stream_handle())
 
     def cau_SCforce(self, lb_field):
         lb_field._sync_fused()
         L = lb_field._lattice()
-        _capi.call("lbm_sc_force", ctypes.byref(L), float(self.g_coh), self.group.ptr,
+        _capi.call("lbm_sc_force", ctypes.byref(L), float(self.g_coh), self.group.on(lb_field).ptr,
                    self.group.n, stream_handle())
 
 
@@ -179,7 +179,7 @@ class FixedPsi(BoundaryCondition):
 
     def apply(self, lb_field):
         L = lb_field._lattice()
-        _capi.call("lbm_psi_fixed", ctypes.byref(L), self.group.ptr, self.group.n,
+        _capi.call("lbm_psi_fixed", ctypes.byref(L), self.group.on(lb_field, halo=1).ptr, self.group.n,
                    float(self.psi_value), stream_handle())
 
 
