@@ -51,18 +51,21 @@ template <>
 struct Storage<LBM_STORE_F32> {
   using T = float;
   static __device__ __forceinline__ float dec(T v, float) { return v; }
+  static __device__ __forceinline__ double dec64(T v, float) { return (double)v; }
   static __device__ __forceinline__ T enc(float v, float) { return v; }
 };
 template <>
 struct Storage<LBM_STORE_F16S> {
   using T = __half;
   static __device__ __forceinline__ float dec(T v, float w) { return __half2float(v) + w; }
+  static __device__ __forceinline__ double dec64(T v, float w) { return (double)__half2float(v) + (double)w; }
   static __device__ __forceinline__ T enc(float v, float w) { return __float2half_rn(v - w); }
 };
 template <>
 struct Storage<LBM_STORE_BF16S> {
   using T = __nv_bfloat16;
   static __device__ __forceinline__ float dec(T v, float w) { return __bfloat162float(v) + w; }
+  static __device__ __forceinline__ double dec64(T v, float w) { return (double)__bfloat162float(v) + (double)w; }
   static __device__ __forceinline__ T enc(float v, float w) { return __float2bfloat16_rn(v - w); }
 };
 
@@ -485,17 +488,13 @@ __global__ void __launch_bounds__(REDUCE_TPB) k_reduce_partial(const FusedParams
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
     const int x = (int)(q % p.pitch);
     if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
-    float m0 = 0.0f, mx = 0.0f, my = 0.0f;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const float v = S::dec(src[(size_t)k * p.plane + q], W(k));
-      m0 += v;
-      mx += (float)CX(k) * v;
-      my += (float)CY(k) * v;
+      const double v = S::dec64(src[(size_t)k * p.plane + q], W(k));
+      a0 += v;
+      if (CX(k)) a1 += CX(k) * v;
+      if (CY(k)) a2 += CY(k) * v;
     }
-    a0 += m0;
-    a1 += mx;
-    a2 += my;
   }
   __shared__ double sh[3][REDUCE_TPB / 32];
   a0 = warp_sum(a0);

@@ -31,6 +31,26 @@ def tol_for(meta):
     return TOL_PL if meta["step_kind"] == "powerlaw" else TOL
 
 
+def fp64_solution(meta, arrays, steps=None):
+    m = dict(meta, fp="f64")
+    return O.replay(m, {k: (v.astype(np.float64) if v.dtype == np.float32 else v)
+                        for k, v in arrays.items()}, steps=steps)
+
+
+def check_parity(got, ref32, ref64, keys, tol):
+    """got (GPU, fp32) vs the fp32 reference: within tol, or within 3x the
+    fp32 reference's own distance from the fp64 solution when that rounding
+    floor is larger (fields whose magnitude is near zero, e.g. u ~ 1e-4);
+    and no further from the fp64 solution than that."""
+    for k in keys:
+        floor = rel_err(ref32[k], ref64[k])
+        bound = max(tol, 3.0 * floor)
+        e32 = rel_err(got[k], ref32[k])
+        e64 = rel_err(got[k], ref64[k])
+        assert e32 <= bound, f"{k}: {e32:.2e} vs fp32 reference (bound {bound:.2e}, floor {floor:.2e})"
+        assert e64 <= bound, f"{k}: {e64:.2e} vs fp64 solution (bound {bound:.2e}, floor {floor:.2e})"
+
+
 @pytest.mark.parametrize("name", sorted(set(fixture_names()) - F64_CASES))
 def test_staged_matches_reference_fixture(tl, name):
     meta, arrays = load_fixture(name)
@@ -38,11 +58,8 @@ def test_staged_matches_reference_fixture(tl, name):
     run_staged(lb, me, coll, be, sc, bsc, meta["step_kind"], meta["steps"])
     torch.cuda.synchronize()
     got = fields_of(lb)
-    tol = tol_for(meta)
-    for k in ("f", "f2", "rho", "vel", "pressure"):
-        assert rel_err(got[k], arrays[k]) < tol, (k, rel_err(got[k], arrays[k]))
-    if "psi" in got:
-        assert rel_err(got["psi"], arrays["psi"]) < tol
+    keys = ["f", "f2", "rho", "vel", "pressure"] + (["psi"] if "psi" in got else [])
+    check_parity(got, arrays, fp64_solution(meta, arrays), keys, tol_for(meta))
 
 
 @pytest.mark.parametrize("name", sorted(set(fixture_names()) - F64_CASES - SC_CASES))
@@ -52,10 +69,8 @@ def test_fused_matches_reference_fixture(tl, name):
     solver = tl.FusedSolver(lb, me, coll, be)
     solver.step(meta["steps"])
     torch.cuda.synchronize()
-    got = fields_of(lb)
-    tol = tol_for(meta)
-    for k in ("f", "f2", "rho", "vel"):
-        assert rel_err(got[k], arrays[k]) < tol, (k, rel_err(got[k], arrays[k]))
+    check_parity(fields_of(lb), arrays, fp64_solution(meta, arrays), ("f", "f2", "rho", "vel"),
+                 tol_for(meta))
 
 
 def test_value_fn_inlet_equals_per_node_boundaries(tl):
@@ -65,9 +80,7 @@ def test_value_fn_inlet_equals_per_node_boundaries(tl):
     lb, me, coll, be, _, _ = build_from_case(tl, meta, arrays, value_fn_inlet=True)
     assert sum(1 for n in be.boundary_conditions if n.startswith("inlet")) == 1
     tl.FusedSolver(lb, me, coll, be).step(meta["steps"])
-    got = fields_of(lb)
-    for k in ("f", "rho", "vel"):
-        assert rel_err(got[k], arrays[k]) < TOL
+    check_parity(fields_of(lb), arrays, fp64_solution(meta, arrays), ("f", "rho", "vel"), TOL)
 
 
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
@@ -81,10 +94,8 @@ def test_fused_matches_oracle_cylinder(tl, model, shape):
                                         model=model, mrt_s=s)
     meta, arrays = describe(lb, coll, be, 200)
     tl.FusedSolver(lb, me, coll, be).step(200)
-    ref = O.replay(meta, arrays)
-    got = fields_of(lb)
-    for k in ("f", "rho", "vel"):
-        assert rel_err(got[k], ref[k]) < 2 * TOL, (k, rel_err(got[k], ref[k]))
+    check_parity(fields_of(lb), O.replay(meta, arrays), fp64_solution(meta, arrays),
+                 ("f", "rho", "vel"), TOL)
 
 
 def test_fused_periodic_box_odd_width(tl):
@@ -112,10 +123,8 @@ def test_fused_periodic_box_odd_width(tl):
     lb.init_LBM(coll, fl.group)
     meta, arrays = describe(lb, coll, be, 150)
     tl.FusedSolver(lb, me, coll, be).step(150)
-    ref = O.replay(meta, arrays)
-    got = fields_of(lb)
-    for k in ("f", "rho", "vel"):
-        assert rel_err(got[k], ref[k]) < 2 * TOL, (k, rel_err(got[k], ref[k]))
+    check_parity(fields_of(lb), O.replay(meta, arrays), fp64_solution(meta, arrays),
+                 ("f", "rho", "vel"), TOL)
 
 
 def test_fused_equals_staged_and_run_is_resumable(tl):
