@@ -262,6 +262,20 @@ int lbm_plan_import(LbmPlan* plan, const float* f_post, void* stream);
 int lbm_plan_export(LbmPlan* plan, float* f_post, void* stream);
 int lbm_plan_destroy(LbmPlan* plan);
 
+/* ----------------------------------------------------------- drag / lift
+ * Not in the reference (it has no force evaluation): momentum exchange on
+ * half-way bounce-back links into solid nodes.  links holds n pairs
+ * (q, k): q = j*pitch + i of a colliding node whose link k points into a
+ * solid neighbour (i + cx_k, j + cy_k); the force on the body from the
+ * current post-collision state is sum 2 c_k f_k(q), accumulated in FP64 and
+ * written to out[0..1] (Fx, Fy). */
+int lbm_plan_momentum_exchange(LbmPlan* plan, const int32_t* links, int64_t n, double* out,
+                               void* stream);
+/* lbm_plan_run followed, after every launch, by the momentum exchange into
+ * series[2*s .. 2*s+1] for step s (series holds nsteps x 2 doubles). */
+int lbm_plan_run_monitored(LbmPlan* plan, int32_t nsteps, const int32_t* links, int64_t n,
+                           double* series, void* stream);
+
 /* ----------------------------------------------------------- reductions
  * FP64 sums over the nodes whose code has LBM_CODE_ACTIVE, of the current
  * population state: out[0] = sum f, out[1] = sum f c_x, out[2] = sum f c_y.

@@ -468,6 +468,45 @@ __global__ void k_convert(const FusedParams p, const float* in, void* out, int t
   }
 }
 
+// Momentum exchange on links into a solid (Ladd): a post-collision
+// population f_k(x) heading into a solid neighbour x + c_k returns as
+// f_opp(k)(x) = f_k(x) (half-way bounce-back), handing the body 2 c_k f_k(x).
+// links: (plane-offset q, k) pairs; one block, FP64 accumulation; writes
+// (Fx, Fy) to out.
+constexpr int MEX_TPB = 256;
+
+template <int ST>
+__global__ void __launch_bounds__(MEX_TPB) k_momentum_exchange(const FusedParams p, const int32_t* links,
+                                                               int64_t n, double* out) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  double fx = 0.0, fy = 0.0;
+  for (int64_t m = threadIdx.x; m < n; m += blockDim.x) {
+    const int64_t q = links[2 * m];
+    const int k = links[2 * m + 1];
+    const double v = S::dec64(src[(size_t)k * p.plane + q], w_dyn(k));
+    fx += 2.0 * cx_dyn(k) * v;
+    fy += 2.0 * cy_dyn(k) * v;
+  }
+  __shared__ double sh[2][MEX_TPB / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    fx += __shfl_down_sync(0xffffffffu, fx, o);
+    fy += __shfl_down_sync(0xffffffffu, fy, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = fx;
+    sh[1][threadIdx.x >> 5] = fy;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double s = 0.0;
+    for (int i = 0; i < MEX_TPB / 32; ++i) s += sh[threadIdx.x][i];
+    out[threadIdx.x] = s;
+  }
+}
+
 // FP64 sums of f, f c_x, f c_y over colliding nodes of the state p.src.
 constexpr int REDUCE_BLOCKS = 152 * 4;
 constexpr int REDUCE_TPB = 256;

@@ -48,9 +48,16 @@ int launch_reduce(const FusedParams& p, double* partials, double* out, cudaStrea
   return lbm_err::launch("moment reduction");
 }
 
+template <int ST>
+int launch_momentum_exchange(const FusedParams& p, const int32_t* links, int64_t n, double* out,
+                             cudaStream_t s) {
+  k_momentum_exchange<ST><<<1, MEX_TPB, 0, s>>>(p, links, n, out);
+  return lbm_err::launch("momentum exchange");
+}
+
 }  // namespace lbm
 
-#define LBM_INSTANTIATE_STORAGE(ST, VA, VB)                                                     \
+#define LBM_INSTANTIATE_STORAGE(ST, VA, VB)                                                    \
   namespace lbm {                                                                               \
   template <>                                                                                   \
   int launch_fused<ST>(const FusedParams& p, int V, cudaStream_t s) {                           \
@@ -61,4 +68,6 @@ int launch_reduce(const FusedParams& p, double* partials, double* out, cudaStrea
   template int launch_stream_only<ST>(const FusedParams&, float*, cudaStream_t);                \
   template int launch_convert<ST>(const FusedParams&, const float*, void*, int, cudaStream_t);  \
   template int launch_reduce<ST>(const FusedParams&, double*, double*, cudaStream_t);           \
+  template int launch_momentum_exchange<ST>(const FusedParams&, const int32_t*, int64_t, double*, \
+                                            cudaStream_t);                                      \
   }

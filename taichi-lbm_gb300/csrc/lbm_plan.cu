@@ -188,6 +188,38 @@ int lbm_plan_destroy(LbmPlan* pl) {
   return LBM_OK;
 }
 
+static int mex(LbmPlan* pl, const int32_t* links, int64_t n, double* out, cudaStream_t s) {
+  FusedParams p = params_for(pl);
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return lbm::launch_momentum_exchange<LBM_STORE_F32>(p, links, n, out, s);
+    case LBM_STORE_F16S: return lbm::launch_momentum_exchange<LBM_STORE_F16S>(p, links, n, out, s);
+    default: return lbm::launch_momentum_exchange<LBM_STORE_BF16S>(p, links, n, out, s);
+  }
+}
+
+int lbm_plan_momentum_exchange(LbmPlan* pl, const int32_t* links, int64_t n, double* out, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "momentum_exchange: plan not bound");
+  if (!out || n < 0 || (n > 0 && !links)) return lbm_err::set(LBM_ERR_ARG, "momentum_exchange: bad arguments");
+  return mex(pl, links, n, out, (cudaStream_t)stream);
+}
+
+int lbm_plan_run_monitored(LbmPlan* pl, int32_t nsteps, const int32_t* links, int64_t n, double* series,
+                           void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "run_monitored: plan not bound");
+  if (nsteps < 0 || !series || n < 0 || (n > 0 && !links))
+    return lbm_err::set(LBM_ERR_ARG, "run_monitored: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int32_t st = 0; st < nsteps; ++st) {
+    FusedParams p = params_for(pl);
+    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, s);
+    if (rc) return rc;
+    pl->parity ^= 1;
+    rc = mex(pl, links, n, series + 2 * (size_t)st, s);
+    if (rc) return rc;
+  }
+  return LBM_OK;
+}
+
 int64_t lbm_reduce_scratch_doubles(void) { return (int64_t)lbm::REDUCE_BLOCKS * 3; }
 
 int lbm_plan_reduce_moments(LbmPlan* pl, double* partials, double* out, void* stream) {

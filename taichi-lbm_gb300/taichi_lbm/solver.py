@@ -250,15 +250,62 @@ class FusedSolver:
         A.call("lbm_plan_get_parity", self._plan, ctypes.byref(par))
         return par.value
 
-    def step(self, n=1):
-        """n reference steps (n calls of lbm_solve()) + the next moment prologue."""
+    def step(self, n=1, forces=False):
+        """n reference steps (n calls of lbm_solve()) + the next moment prologue.
+
+        forces=True also returns the force on the solid obstacles after each
+        step's collision (momentum exchange on bounce-back links into mask=-1
+        nodes): an (n, 2) float64 CUDA tensor, row s = step s+1."""
         n = int(n)
         if n <= 0:
-            return
+            return None
         self.begin()
-        if n > 1:
+        series = None
+        if forces:
+            links = self.solid_links()
+            series = torch.zeros((n, 2), dtype=torch.float64, device=self.lb.device)
+            lp, ln = ctypes.c_void_p(links.data_ptr()), links.shape[0]
+            s = stream_handle()
+            A.call("lbm_plan_momentum_exchange", self._plan, lp, ln,
+                   ctypes.c_void_p(series.data_ptr()), s)
+            if n > 1:
+                A.call("lbm_plan_run_monitored", self._plan, n - 1, lp, ln,
+                       ctypes.c_void_p(series[1:].data_ptr()), s)
+        elif n > 1:
             self.run(n - 1)
         self.finish()
+        return series
+
+    def solid_links(self):
+        """(m, 2) int32 device tensor of (j*pitch + i, k): colliding node and
+        outgoing link k whose neighbour (i + cx_k, j + cy_k) is a solid node
+        reached through a bounce-back link."""
+        if getattr(self, "_solid_links", None) is not None:
+            return self._solid_links
+        lb = self.lb
+        code = self.compiled.code.astype(np.int64)
+        mask = lb.mask.arr
+        nx, ny = lb.NX, lb.NY
+        I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+        cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+        opp = [0, 3, 4, 1, 2, 7, 8, 5, 6]
+        rows = []
+        active = (code & A.CODE_ACTIVE) != 0
+        for kp in range(1, 9):
+            k = opp[kp]
+            i2, j2 = I + cx[k], J + cy[k]
+            inside = (i2 >= 0) & (i2 < nx) & (j2 >= 0) & (j2 < ny)
+            solid = np.zeros_like(inside)
+            solid[inside] = mask[i2[inside], j2[inside]] == -1
+            sel = active & ((code >> (kp - 1)) & 1 == 1) & solid
+            ii, jj = I[sel], J[sel]
+            rows.append(np.stack([jj * lb.pitch + ii, np.full_like(ii, k)], 1))
+        links = np.concatenate(rows).astype(np.int32) if rows else np.zeros((0, 2), np.int32)
+        t = torch.as_tensor(links if links.size else np.zeros((1, 2), np.int32), device=lb.device)
+        self._solid_links = t[:links.shape[0]] if links.size else t[:0]
+        self._solid_links_host = links
+        return self._solid_links
 
     def reduce_moments(self):
         """FP64 (sum f, sum f cx, sum f cy) over colliding nodes of the live

@@ -176,3 +176,26 @@ def test_fp64_mass_reduction(tl):
     s.finish()
     assert abs(out[0] - exp[0]) / exp[0] < 1e-12
     assert abs(out[1] - exp[1]) < 1e-9 and abs(out[2] - exp[2]) < 1e-9
+
+
+def test_drag_lift_series_matches_oracle(tl):
+    """Momentum-exchange force on the cylinder after every step, fused path
+    vs the same sum over the oracle's post-collision populations."""
+    lb, me, coll, be = cylinder_channel(tl, 200, 60, 6.0, 40.0, 29.5, 0.6, 0.05)
+    meta, arrays = describe(lb, coll, be, 80)
+    s = tl.FusedSolver(lb, me, coll, be)
+    series = s.step(80, forces=True).cpu().numpy()
+    links = s._solid_links_host
+    assert links.shape[0] > 20
+    i, j, k = links[:, 0] % lb.pitch, links[:, 0] // lb.pitch, links[:, 1]
+    c = np.array([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]])
+    run = O.prepare(meta, arrays)
+    ref = []
+    for _ in range(80):
+        run.step(1)
+        v = run.o.field("f2")[i, j, k].astype(np.float64)
+        ref.append([(2 * c[k, 0] * v).sum(), (2 * c[k, 1] * v).sum()])
+    run.finish()
+    ref = np.array(ref)
+    assert np.abs(series - ref).max() / np.abs(ref).max() < 1e-4
+    assert series[-1, 0] > 0  # drag points downstream
