@@ -283,6 +283,24 @@ int lbm_plan_run_monitored(LbmPlan* plan, int32_t nsteps, const int32_t* links, 
 int64_t lbm_reduce_scratch_doubles(void);
 int lbm_plan_reduce_moments(LbmPlan* plan, double* partials, double* out, void* stream);
 
+/* Allocation-free lbm_plan_reduce_moments (no counterpart in taichi-lbm,
+ * which has no reductions at all).  For callers that cannot allocate device
+ * memory themselves: a host whose device memory is all handed out by its own
+ * pool or budget (a serving loop admitting lattices against an HBM budget
+ * has no spare buffer to lend), or a monitor hook between steps that must
+ * not trigger cudaMalloc and the device synchronisation it implies.
+ * The caller passes only the plan (its bound state is the input) and out.
+ * Scratch is a 48 KiB file-scope __device__ array that every GPU which loads
+ * the library holds until process exit.  The first call on each device looks
+ * its device address up (cudaGetSymbolAddress) with that device current, so
+ * make that first call before any stream capture.  Lattices with more than
+ * LBM_NOALLOC_MAX_NODES sites (ny * pitch) are rejected with LBM_ERR_ARG.
+ * Every call shares the array: calls that overlap on the GPU race.  No
+ * cudaMalloc, cudaFree or allocating library routine is called. */
+#define LBM_NOALLOC_CHUNK 16384LL
+#define LBM_NOALLOC_MAX_NODES (2048LL * LBM_NOALLOC_CHUNK)
+int lbm_plan_reduce_moments_noalloc(LbmPlan* plan, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

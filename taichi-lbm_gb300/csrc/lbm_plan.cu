@@ -1,5 +1,6 @@
 // Fused-step plans: validation, buffer binding and stream-ordered launches.
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "lbm_fused_launch.cuh"
@@ -218,6 +219,123 @@ int lbm_plan_run_monitored(LbmPlan* pl, int32_t nsteps, const int32_t* links, in
     if (rc) return rc;
   }
   return LBM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------
+// Allocation-free moment reduction.
+//
+// For callers that must not allocate device memory themselves: the partial
+// sums live in this file-scope device array instead of caller scratch.  It is
+// 3 * LBM_NOALLOC_BLOCKS doubles (48 KiB) on every device that loads the
+// library and stays allocated until the process exits.  Each block reduces a
+// fixed chunk of LBM_NOALLOC_CHUNK lattice sites, so the largest lattice the
+// array serves is LBM_NOALLOC_MAX_NODES sites (ny * pitch); larger ones are
+// rejected.  All calls share the array and every call overwrites the slots
+// it reads, so nothing needs clearing; calls whose work overlaps on the GPU
+// (different streams or threads) race on it.
+namespace {
+
+static_assert(LBM_NOALLOC_MAX_NODES % LBM_NOALLOC_CHUNK == 0, "chunk must divide the limit");
+constexpr int LBM_NOALLOC_BLOCKS = (int)(LBM_NOALLOC_MAX_NODES / LBM_NOALLOC_CHUNK);
+
+__device__ __align__(256) double g_noalloc_partials[3 * LBM_NOALLOC_BLOCKS];
+
+// Host code cannot use g_noalloc_partials as a pointer: its host-side name is
+// a stand-in, not the device address.  The address is looked up once per
+// device, with that device current, on the first call made on it.
+constexpr int MAX_DEVICES = 64;
+double* g_noalloc_ptr[MAX_DEVICES] = {nullptr};
+std::mutex g_noalloc_mutex;
+
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  int rc = lbm_err::cuda(cudaGetDevice(&dev), "noalloc reduction: cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= MAX_DEVICES) return lbm_err::set(LBM_ERR_UNSUPPORTED, "device ordinal %d", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    rc = lbm_err::cuda(cudaGetSymbolAddress(&p, g_noalloc_partials),
+                       "noalloc reduction: cudaGetSymbolAddress");
+    if (rc) return rc;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return LBM_OK;
+}
+
+// block b sums sites [b*chunk, (b+1)*chunk) of the state into partials[3b..3b+2]
+template <int ST>
+__global__ void __launch_bounds__(lbm::REDUCE_TPB) k_reduce_chunked(const FusedParams p, double* partials,
+                                                                    int64_t chunk) {
+  using S = lbm::Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  const size_t n = (size_t)p.ny * p.pitch;
+  const size_t lo = (size_t)blockIdx.x * chunk;
+  const size_t hi = lo + chunk < n ? lo + chunk : n;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (size_t q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+    const int x = (int)(q % p.pitch);
+    if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const double v = S::dec64(src[(size_t)k * p.plane + q], lbm::W(k));
+      a0 += v;
+      if (lbm::CX(k)) a1 += lbm::CX(k) * v;
+      if (lbm::CY(k)) a2 += lbm::CY(k) * v;
+    }
+  }
+  __shared__ double sh[3][lbm::REDUCE_TPB / 32];
+  a0 = lbm::warp_sum(a0);
+  a1 = lbm::warp_sum(a1);
+  a2 = lbm::warp_sum(a2);
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = a0;
+    sh[1][threadIdx.x >> 5] = a1;
+    sh[2][threadIdx.x >> 5] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int i = 0; i < lbm::REDUCE_TPB / 32; ++i) s += sh[threadIdx.x][i];
+    partials[(size_t)blockIdx.x * 3 + threadIdx.x] = s;
+  }
+}
+
+template <int ST>
+int launch_noalloc(const FusedParams& p, double* partials, int nblocks, double* out, cudaStream_t s) {
+  k_reduce_chunked<ST><<<nblocks, lbm::REDUCE_TPB, 0, s>>>(p, partials, LBM_NOALLOC_CHUNK);
+  lbm::k_reduce_final<ST><<<1, 96, 0, s>>>(partials, nblocks, out);
+  return lbm_err::launch("noalloc moment reduction");
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_plan_reduce_moments_noalloc(LbmPlan* pl, double* out, void* stream) {
+  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "reduce_noalloc: plan not bound");
+  if (!out) return lbm_err::set(LBM_ERR_ARG, "reduce_noalloc: NULL output");
+  const int64_t sites = (int64_t)pl->d.ny * pl->d.pitch;
+  if (sites > LBM_NOALLOC_MAX_NODES)
+    return lbm_err::set(LBM_ERR_ARG,
+                        "reduce_noalloc: lattice of %lld sites (ny * pitch) exceeds the allocation-free "
+                        "limit of %lld; use lbm_plan_reduce_moments with caller scratch",
+                        (long long)sites, (long long)LBM_NOALLOC_MAX_NODES);
+  double* partials = nullptr;
+  int rc = noalloc_scratch(&partials);
+  if (rc) return rc;
+  const int nblocks = (int)((sites + LBM_NOALLOC_CHUNK - 1) / LBM_NOALLOC_CHUNK);
+  FusedParams p = params_for(pl);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return launch_noalloc<LBM_STORE_F32>(p, partials, nblocks, out, s);
+    case LBM_STORE_F16S: return launch_noalloc<LBM_STORE_F16S>(p, partials, nblocks, out, s);
+    default: return launch_noalloc<LBM_STORE_BF16S>(p, partials, nblocks, out, s);
+  }
 }
 
 int64_t lbm_reduce_scratch_doubles(void) { return (int64_t)lbm::REDUCE_BLOCKS * 3; }

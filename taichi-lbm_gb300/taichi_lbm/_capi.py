@@ -116,6 +116,7 @@ _SIGS = {
     "lbm_plan_momentum_exchange": ([_vp, _vp, ctypes.c_int64, _vp, _vp], ctypes.c_int),
     "lbm_plan_run_monitored": ([_vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp], ctypes.c_int),
     "lbm_reduce_scratch_doubles": ([], ctypes.c_int64),
+    "lbm_plan_reduce_moments_noalloc": ([_vp, _vp, _vp], ctypes.c_int),
     "lbm_plan_reduce_moments": ([_vp, _vp, _vp, _vp], ctypes.c_int),
 }
 
