@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--nx", type=int, default=CONFIG["nx"])
     ap.add_argument("--ny", type=int, default=CONFIG["ny"])
     ap.add_argument("--nodes-per-thread", type=int, default=None)
+    ap.add_argument("--pipeline", default="direct", choices=["direct", "async"])
     ap.add_argument("--no-extras", action="store_true", help="skip the per-model/storage lines")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -171,12 +172,12 @@ def barrier(dist):
         torch.cuda.synchronize()
 
 
-def build(tl, cfg, model, storage, V):
+def build(tl, cfg, model, storage, V, pipeline="direct"):
     from taichi_lbm.workloads import cylinder_channel
     lb, me, coll, be = cylinder_channel(tl, cfg["nx"], cfg["ny"], cfg["radius"], cfg["cx"], cfg["cy"],
                                         cfg["tau"], cfg["umax"], model=model,
                                         mrt_s=MRT_S if model == "mrt" else None, keep_init=False)
-    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, nodes_per_thread=V)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, nodes_per_thread=V, pipeline=pipeline)
     return lb, me, coll, be, solver
 
 
@@ -262,7 +263,7 @@ def run_ours(a):
     cfg = workload_config(a)
     K, W = a.steps, max(3, a.warmup)
     peak, peak_kind = measured_peak()
-    lb, me, coll, be, solver = build(tl, cfg, a.model, a.storage, a.nodes_per_thread)
+    lb, me, coll, be, solver = build(tl, cfg, a.model, a.storage, a.nodes_per_thread, a.pipeline)
     active = coll.group.n
     ms, clocks = time_resident(solver, K, W, dist, local)
     ms = max_over_ranks(ms, dist)
@@ -282,7 +283,8 @@ def run_ours(a):
                                f"parabolic inlet u_max={cfg['umax']}, PressureNEEM outlet, "
                                "bounce-back walls", "nodes": cfg["nx"] * cfg["ny"],
                    "updated_nodes_per_step": active, "model": a.model, "storage": a.storage,
-                   "nodes_per_thread": solver.V, "parallelism": f"replicas x{ws}",
+                   "nodes_per_thread": solver.V, "pipeline": a.pipeline,
+                   "parallelism": f"replicas x{ws}",
                    "l2": "state (2 x 9 populations) larger than L2; no flush needed"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -303,7 +305,7 @@ def run_ours(a):
         for model, storage in (("trt", "fp32"), ("mrt", "fp32"), ("bgk", "fp16s"), ("bgk", "bf16s")):
             if (model, storage) == (a.model, a.storage):
                 continue
-            lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None)
+            lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None, a.pipeline)
             k2 = max(10, K // 4)
             ms2, _ = time_resident(s2, k2, W, None, local)
             act = coll2.group.n

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define LBM_GB300_ABI_VERSION 1
+#define LBM_GB300_ABI_VERSION 2
 
 enum {
   LBM_OK = 0,
@@ -229,7 +229,36 @@ typedef struct LbmPlanDesc {
                                       ignored here (see LbmPlanBuffers)     */
   int32_t nprog;
   int8_t prog[LBM_MAX_PROG][LBM_PROG_LEN]; /* bc indices, -1 terminated     */
+  int32_t pipeline;     /* LBM_PIPE_DIRECT: one warp per row segment, vector
+                           loads into registers;
+                           LBM_PIPE_ASYNC: persistent warps staging source
+                           rows through shared memory with cp.async.bulk
+                           (needs nodes_per_thread == 4 and a status word);
+                           LBM_PIPE_PREFETCH: persistent warps loading the
+                           next segment into registers while colliding the
+                           current one (nodes_per_thread == 4)             */
+  int32_t tune;         /* LBM_PIPE_ASYNC: 0..LBM_ASYNC_TUNINGS-1 selects
+                           (warps per block, stages per warp) =
+                           (8,2) (6,3) (4,4) (16,2)                         */
+  /* Single-component Shan-Chen (ExternalForce.py:122-158) on a fully periodic
+   * lattice: each step computes psi(rho, T) from the post-stream populations,
+   * F = -g_coh psi(x) sum_k w_k c_k psi(x + c_k) + gravity, then collides.
+   * Needs the direct pipeline, nodes_per_thread 4, ny divisible by 8, no
+   * rewrite boundaries and a uniform temperature.                          */
+  int32_t sc;
+  float g_coh;
+  float sc_T;
+  LbmEos eos;
+  /* 16-bit storages (LBM_STORE_F16S / BF16S) hold f_k - w_k * rho_ref so the
+   * stored value is the small deviation from rest at density rho_ref; choose
+   * the lattice's mean density (0 is read as 1).  Ignored for fp32.        */
+  float rho_ref;
 } LbmPlanDesc;
+
+enum { LBM_PIPE_DIRECT = 0, LBM_PIPE_ASYNC = 1, LBM_PIPE_PREFETCH = 2 };
+#define LBM_ASYNC_TUNINGS 4
+/* *status (LbmPlanBuffers.status) after an async step: 0, or 1 when a wait on
+ * a copy exceeded its time budget (the step's output is then invalid). */
 
 typedef struct LbmPlanBuffers {
   void* fa;             /* [9][ny][pitch] populations, element type per storage */
@@ -242,6 +271,13 @@ typedef struct LbmPlanBuffers {
   const float* bc_vel;  /* [2][ny][pitch] per-node boundary velocity or NULL */
   float* tau;           /* [ny][pitch] power-law state (BGK tau, TRT tau_sym,
                            MRT diag[7]) or NULL                              */
+  int32_t* status;      /* one device int32 (LBM_PIPE_ASYNC), else NULL     */
+  /* LBM_PIPE_DIRECT only, optional: the indices (y * nseg + seg, ascending)
+   * of every segment whose seg_flags entry is nonzero.  With it a step is two
+   * launches, a lean kernel over the plain segments and a general one over
+   * the listed segments; NULL keeps one general launch per step.          */
+  const int32_t* special;
+  int32_t nspecial;
 } LbmPlanBuffers;
 
 typedef struct LbmPlan LbmPlan;

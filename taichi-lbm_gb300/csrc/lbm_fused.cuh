@@ -42,6 +42,18 @@ struct FusedParams {
   int nbc;
   LbmBoundary bc[LBM_MAX_BC];
   int8_t prog[LBM_MAX_PROG][LBM_PROG_LEN];
+  // single-component Shan-Chen (k_fused_sc): interaction strength, the
+  // lattice's uniform temperature and the pseudopotential
+  int sc;
+  float g_coh, sc_T;
+  LbmEos eos;
+  // two-pass direct step: segments with a nonzero flag, in (y * nseg + seg)
+  // order, handled by k_fused_special; k_fused_bulk skips them
+  const int32_t* special;
+  int nspecial;
+  // 16-bit storage holds f_k - wsh[k], wsh[k] = w_k * rho_ref (the plan's
+  // reference density); fp32 storage ignores it
+  float wsh[9];
 };
 
 // ------------------------------------------------------------ storage
@@ -132,10 +144,10 @@ __device__ __forceinline__ void gather_node(const FusedParams& p, int x, int y, 
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     if (k > 0 && (code & (1u << (k - 1)))) {
-      g[k] = S::dec(load1(src + OPP(k) * p.plane + (size_t)y * p.pitch + x), W(OPP(k)));
+      g[k] = S::dec(load1(src + OPP(k) * p.plane + (size_t)y * p.pitch + x), p.wsh[OPP(k)]);
     } else {
       const int xs = wrap(x - CX(k), p.nx), ys = wrap(y - CY(k), p.ny);
-      g[k] = S::dec(load1(src + k * p.plane + (size_t)ys * p.pitch + xs), W(k));
+      g[k] = S::dec(load1(src + k * p.plane + (size_t)ys * p.pitch + xs), p.wsh[k]);
     }
   }
 }
@@ -247,9 +259,11 @@ namespace lbm {
 
 // Relaxation + collision of one node in place; returns the new relaxation
 // state (power law) or the old one.
-template <int MODEL, bool PL>
+// FORCE: 1 / 0 = body force on / off at compile time, -1 = read p.has_force
+template <int MODEL, bool PL, int FORCE = -1>
 __device__ __forceinline__ float relax_collide(const FusedParams& p, float f[9], float rho, float ux, float uy,
                                                float Fx, float Fy, float state) {
+  const bool force = FORCE < 0 ? p.has_force != 0 : FORCE == 1;
   if (MODEL == LBM_MRT) {
     float s[9];
 #pragma unroll
@@ -271,7 +285,7 @@ __device__ __forceinline__ float relax_collide(const FusedParams& p, float f[9],
       state = 1.0f / t;
       s[7] = s[8] = state;
     }
-    collide_mrt(f, rho, ux, uy, Fx, Fy, s, p.has_force);
+    collide_mrt(f, rho, ux, uy, Fx, Fy, s, force);
     return state;
   }
   float om = p.omega, oa = p.omega_a;
@@ -287,28 +301,80 @@ __device__ __forceinline__ float relax_collide(const FusedParams& p, float f[9],
     om = 1.0f / t;
     if (MODEL == LBM_TRT) oa = 1.0f / (p.magic / (t - 0.5f) + 0.5f);
   }
-  if (MODEL == LBM_BGK) collide_bgk(f, rho, ux, uy, Fx, Fy, om, p.has_force);
-  else collide_trt(f, rho, ux, uy, Fx, Fy, om, oa, p.has_force);
+  if (MODEL == LBM_BGK) collide_bgk(f, rho, ux, uy, Fx, Fy, om, force);
+  else collide_trt(f, rho, ux, uy, Fx, Fy, om, oa, force);
   return state;
 }
 
+// GENERAL = false: the segment is known to be plain (no per-node codes);
+// FORCE as in relax_collide
+template <int MODEL, bool PL, int ST, int V, bool GENERAL = true, int FORCE = -1>
+__device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9], int y, int seg, int x0,
+                                           bool live);
+
+template <int ST, int V>
+__device__ __forceinline__ void gather_direct(const FusedParams& p, int y, int seg, int lane, float (&f)[V][9]);
+
 template <int MODEL, bool PL, int ST, int V>
 __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
-  using S = Storage<ST>;
-  using T = typename S::T;
-  constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= (long long)p.ny * p.nseg) return;  // whole warps only
   const int y = (int)(warp / p.nseg);
   const int seg = (int)(warp - (long long)y * p.nseg);
   const int x0 = seg * 32 * V + lane * V;
+  float f[V][9];
+  gather_direct<ST, V>(p, y, seg, lane, f);
+  fused_tail<MODEL, PL, ST, V>(p, f, y, seg, x0, x0 < p.nx);
+}
+
+// Two-pass form of the same step.  k_fused_bulk takes the plain segments
+// (seg_flags == 0: every node collides and streams all nine links, no
+// boundary program, no saved moments), with the body force fixed at compile
+// time, and leaves the flagged segments to k_fused_special, which walks the
+// compact list p.special of their indices (y * nseg + seg).  The two write
+// disjoint nodes and read only the source state, so their order within a
+// step is free.
+template <int MODEL, bool PL, int ST, int V, int FORCE>
+__global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= (long long)p.ny * p.nseg) return;
+  if (p.seg_flags[warp]) return;  // uniform over the warp
+  const int y = (int)(warp / p.nseg);
+  const int seg = (int)(warp - (long long)y * p.nseg);
+  const int x0 = seg * 32 * V + lane * V;
+  float f[V][9];
+  gather_direct<ST, V>(p, y, seg, lane, f);
+  fused_tail<MODEL, PL, ST, V, false, FORCE>(p, f, y, seg, x0, x0 < p.nx);
+}
+
+template <int MODEL, bool PL, int ST, int V>
+__global__ void __launch_bounds__(256) k_fused_special(const FusedParams p) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= p.nspecial) return;
+  const int item = p.special[warp];
+  const int y = item / p.nseg;
+  const int seg = item - y * p.nseg;
+  const int x0 = seg * 32 * V + lane * V;
+  float f[V][9];
+  gather_direct<ST, V>(p, y, seg, lane, f);
+  fused_tail<MODEL, PL, ST, V>(p, f, y, seg, x0, x0 < p.nx);
+}
+
+// Pull-stream gather of one row segment (32*V nodes, V per lane): one aligned
+// V-wide load per population, +-1 x shifts by warp shuffles, the segment-edge
+// elements by lane 0 / lane 31, and node nx-1's wrap-around fix-up.
+template <int ST, int V>
+__device__ __forceinline__ void gather_direct(const FusedParams& p, int y, int seg, int lane, float (&f)[V][9]) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int x0 = seg * 32 * V + lane * V;
   const bool live = x0 < p.nx;
   const int ilast = p.nx - 1 - x0;  // index of node nx-1 in this chunk, if in [0, V)
   const T* src = reinterpret_cast<const T*>(p.src);
-  const size_t rowoff = (size_t)y * p.pitch;
-
-  float f[V][9];
   // ---- pull-stream gather: one aligned V-wide load per population
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
@@ -318,7 +384,7 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
       T raw[V];
       load_vec<T, V>(row + x0, raw);
 #pragma unroll
-      for (int i = 0; i < V; ++i) c[i] = S::dec(raw[i], W(k));
+      for (int i = 0; i < V; ++i) c[i] = S::dec(raw[i], p.wsh[k]);
     } else {
 #pragma unroll
       for (int i = 0; i < V; ++i) c[i] = 0.0f;
@@ -328,27 +394,38 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
       for (int i = 0; i < V; ++i) f[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0 && live) left = S::dec(load1(row + wrap(x0 - 1, p.nx)), W(k));
+      if (lane == 0 && live) left = S::dec(load1(row + wrap(x0 - 1, p.nx)), p.wsh[k]);
       f[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) f[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31 && live) right = S::dec(load1(row + wrap(x0 + V, p.nx)), W(k));
+      if (lane == 31 && live) right = S::dec(load1(row + wrap(x0 + V, p.nx)), p.wsh[k]);
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) f[i][k] = c[i + 1];
       f[V - 1][k] = right;
       if (live && ilast < V) {  // node nx-1 pulls from column 0
-        const float v0 = S::dec(load1(row), W(k));
+        const float v0 = S::dec(load1(row), p.wsh[k]);
 #pragma unroll
         for (int i = 0; i < V; ++i)
           if (i == ilast) f[i][k] = v0;
       }
     }
   }
+}
 
+// After the gather: the per-node path (bounce-back links, boundary
+// programs), moments, relaxation, collision and the stores of one lane's V
+// x-consecutive nodes starting at x0 in row y.
+template <int MODEL, bool PL, int ST, int V, bool GENERAL, int FORCE>
+__device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9], int y, int seg, int x0,
+                                           bool live) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  const size_t rowoff = (size_t)y * p.pitch;
   // ---- per-node path: bounce-back links, boundary programs
-  const unsigned flag = p.seg_flags[(size_t)y * p.nseg + seg];
+  const unsigned flag = GENERAL ? p.seg_flags[(size_t)y * p.nseg + seg] : 0u;
   unsigned code[V];
 #pragma unroll
   for (int i = 0; i < V; ++i) code[i] = LBM_CODE_ACTIVE;
@@ -368,7 +445,7 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
 #pragma unroll
         for (int k = 1; k < 9; ++k)
           if (code[i] & (1u << (k - 1)))
-            f[i][k] = S::dec(load1(src + (size_t)OPP(k) * p.plane + rowoff + x0 + i), W(OPP(k)));
+            f[i][k] = S::dec(load1(src + (size_t)OPP(k) * p.plane + rowoff + x0 + i), p.wsh[OPP(k)]);
       }
       const unsigned prog = code[i] >> LBM_CODE_PROG_SHIFT;
       if (prog) {
@@ -396,7 +473,8 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
       for (int i = 0; i < V; ++i) tau[i] = 1.0f;
     }
   }
-  const float Fx = p.has_force ? p.gx : 0.0f, Fy = p.has_force ? p.gy : 0.0f;
+  const bool force = FORCE < 0 ? p.has_force != 0 : FORCE == 1;
+  const float Fx = force ? p.gx : 0.0f, Fy = force ? p.gy : 0.0f;
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     float* fi = f[i];
@@ -410,13 +488,13 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
       p.mom_out[p.plane + q] = ux;
       p.mom_out[2 * p.plane + q] = uy;
     }
-    const float st = relax_collide<MODEL, PL>(p, fi, rho, ux, uy, Fx, Fy, PL ? tau[i] : 0.0f);
+    const float st = relax_collide<MODEL, PL, FORCE>(p, fi, rho, ux, uy, Fx, Fy, PL ? tau[i] : 0.0f);
     if (!(code[i] & LBM_CODE_ACTIVE)) {
       // not in the collision group: its post-collision populations never
       // change (the reference never writes f2 there), so carry them over
       if (live) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), W(k));
+        for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), p.wsh[k]);
       }
     } else if (PL) {
       tau[i] = st;
@@ -429,7 +507,7 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
   for (int k = 0; k < 9; ++k) {
     T raw[V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], W(k));
+    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], p.wsh[k]);
     store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
   }
 }
@@ -462,7 +540,7 @@ __global__ void k_convert(const FusedParams p, const float* in, void* out, int t
   const size_t n = 9 * p.plane;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const int k = (int)(t / p.plane);
-    const float w = k == 0 ? W(0) : (k <= 4 ? W(1) : W(5));
+    const float w = p.wsh[k];
     if (to_storage) reinterpret_cast<T*>(out)[t] = S::enc(in[t], w);
     else reinterpret_cast<float*>(out)[t] = S::dec(reinterpret_cast<const T*>(p.src)[t], w);
   }
@@ -485,7 +563,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_momentum_exchange(const FusedParams
   for (int64_t m = threadIdx.x; m < n; m += blockDim.x) {
     const int64_t q = links[2 * m];
     const int k = links[2 * m + 1];
-    const double v = S::dec64(src[(size_t)k * p.plane + q], w_dyn(k));
+    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
     fx += 2.0 * cx_dyn(k) * v;
     fy += 2.0 * cy_dyn(k) * v;
   }
@@ -529,7 +607,7 @@ __global__ void __launch_bounds__(REDUCE_TPB) k_reduce_partial(const FusedParams
     if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double v = S::dec64(src[(size_t)k * p.plane + q], W(k));
+      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
       a0 += v;
       if (CX(k)) a1 += CX(k) * v;
       if (CY(k)) a2 += CY(k) * v;

@@ -3,14 +3,130 @@
 #pragma once
 
 #include "lbm_fused.cuh"
+#include "lbm_fused_async.cuh"
+#include "lbm_fused_sc.cuh"
 
 namespace lbm {
+
+template <int ST>
+int launch_fused_sc(const FusedParams& p, cudaStream_t s) {
+  const unsigned blocks = (unsigned)((p.ny / SC_ROWS) * p.nseg);
+  switch (p.model) {
+    case LBM_BGK: k_fused_sc<LBM_BGK, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
+    case LBM_TRT: k_fused_sc<LBM_TRT, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
+    case LBM_MRT: k_fused_sc<LBM_MRT, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
+    default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
+  }
+  return lbm_err::launch("fused Shan-Chen step");
+}
+
+// Grid of a persistent kernel: as many blocks as fit on every SM.
+template <typename K>
+int persistent_blocks(K kern, int threads, int smem, int* blocks) {
+  if (*blocks) return LBM_OK;
+  if (smem > 48 * 1024) {
+    int rc = lbm_err::cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                           "persistent step: shared-memory attribute");
+    if (rc) return rc;
+  }
+  int per_sm = 0, dev = 0, sms = 0;
+  int rc = lbm_err::cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
+                         "persistent step: occupancy");
+  if (rc) return rc;
+  rc = lbm_err::cuda(cudaGetDevice(&dev), "persistent step: device");
+  if (rc) return rc;
+  rc = lbm_err::cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "persistent step: SMs");
+  if (rc) return rc;
+  *blocks = (per_sm > 0 ? per_sm : 1) * sms;
+  return LBM_OK;
+}
+
+template <int MODEL, bool PL, int ST, int NW, int NS>
+int launch_async_mp(const FusedParams& p, int32_t* status, cudaStream_t s) {
+  static int blocks = 0;
+  auto kern = k_fused_async<MODEL, PL, ST, NW, NS>;
+  const int smem = AsyncGeom<ST, NW, NS>::SMEM;
+  int rc = persistent_blocks(kern, NW * 32, smem, &blocks);
+  if (rc) return rc;
+  kern<<<blocks, NW * 32, smem, s>>>(p, status);
+  return lbm_err::launch("fused step (async)");
+}
+
+template <int MODEL, bool PL, int ST>
+int launch_async_tuned(const FusedParams& p, int32_t* status, int tune, cudaStream_t s) {
+  switch (tune) {  // (warps per block, stages per warp)
+    case 0: return launch_async_mp<MODEL, PL, ST, 8, 2>(p, status, s);
+    case 1: return launch_async_mp<MODEL, PL, ST, 6, 3>(p, status, s);
+    case 2: return launch_async_mp<MODEL, PL, ST, 4, 4>(p, status, s);
+    case 3: return launch_async_mp<MODEL, PL, ST, 16, 2>(p, status, s);
+    default: return lbm_err::set(LBM_ERR_ARG, "async tuning %d (0..%d)", tune, LBM_ASYNC_TUNINGS - 1);
+  }
+}
+
+template <int MODEL, bool PL, int ST>
+int launch_prefetch_mp(const FusedParams& p, cudaStream_t s) {
+  static int blocks = 0;
+  auto kern = k_fused_prefetch<MODEL, PL, ST>;
+  int rc = persistent_blocks(kern, 256, 0, &blocks);
+  if (rc) return rc;
+  kern<<<blocks, 256, 0, s>>>(p);
+  return lbm_err::launch("fused step (prefetch)");
+}
+
+// pipeline LBM_PIPE_ASYNC (with tune) or LBM_PIPE_PREFETCH
+template <int ST>
+int launch_fused_persistent(const FusedParams& p, int pipeline, int tune, int32_t* status, cudaStream_t s) {
+  const bool pl = p.fluid_model == LBM_POWERLAW;
+  const int m = p.model * 2 + (pl ? 1 : 0);
+  if (pipeline == LBM_PIPE_PREFETCH) {
+    switch (m) {
+      case 0: return launch_prefetch_mp<LBM_BGK, false, ST>(p, s);
+      case 1: return launch_prefetch_mp<LBM_BGK, true, ST>(p, s);
+      case 2: return launch_prefetch_mp<LBM_TRT, false, ST>(p, s);
+      case 3: return launch_prefetch_mp<LBM_TRT, true, ST>(p, s);
+      case 4: return launch_prefetch_mp<LBM_MRT, false, ST>(p, s);
+      case 5: return launch_prefetch_mp<LBM_MRT, true, ST>(p, s);
+      default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
+    }
+  }
+  switch (m) {
+    case 0: return launch_async_tuned<LBM_BGK, false, ST>(p, status, tune, s);
+    case 1: return launch_async_tuned<LBM_BGK, true, ST>(p, status, tune, s);
+    case 2: return launch_async_tuned<LBM_TRT, false, ST>(p, status, tune, s);
+    case 3: return launch_async_tuned<LBM_TRT, true, ST>(p, status, tune, s);
+    case 4: return launch_async_tuned<LBM_MRT, false, ST>(p, status, tune, s);
+    case 5: return launch_async_tuned<LBM_MRT, true, ST>(p, status, tune, s);
+    default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
+  }
+}
+
+// plain segments with a compile-time force switch, then the listed ones
+template <int MODEL, bool PL, int ST, int V>
+int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s) {
+  if (p.has_force) k_fused_bulk<MODEL, PL, ST, V, 1><<<blocks, 256, 0, s>>>(p);
+  else k_fused_bulk<MODEL, PL, ST, V, 0><<<blocks, 256, 0, s>>>(p);
+  int rc = lbm_err::launch("fused step (plain segments)");
+  if (rc || p.nspecial == 0) return rc;
+  k_fused_special<MODEL, PL, ST, V><<<(unsigned)((p.nspecial + 7) / 8), 256, 0, s>>>(p);
+  return lbm_err::launch("fused step (flagged segments)");
+}
 
 template <int ST, int V>
 int launch_fused_v(const FusedParams& p, cudaStream_t s) {
   const long long warps = (long long)p.ny * p.nseg;
   const unsigned blocks = (unsigned)((warps + 7) / 8);
   const bool pl = p.fluid_model == LBM_POWERLAW;
+  if (p.special) {
+    switch (p.model * 2 + (pl ? 1 : 0)) {
+      case 0: return launch_two_pass<LBM_BGK, false, ST, V>(p, blocks, s);
+      case 1: return launch_two_pass<LBM_BGK, true, ST, V>(p, blocks, s);
+      case 2: return launch_two_pass<LBM_TRT, false, ST, V>(p, blocks, s);
+      case 3: return launch_two_pass<LBM_TRT, true, ST, V>(p, blocks, s);
+      case 4: return launch_two_pass<LBM_MRT, false, ST, V>(p, blocks, s);
+      case 5: return launch_two_pass<LBM_MRT, true, ST, V>(p, blocks, s);
+      default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
+    }
+  }
 #define LBM_LAUNCH_(M, PL) k_fused<M, PL, ST, V><<<blocks, 256, 0, s>>>(p)
   switch (p.model * 2 + (pl ? 1 : 0)) {
     case 0: LBM_LAUNCH_(LBM_BGK, false); break;
@@ -57,6 +173,19 @@ int launch_momentum_exchange(const FusedParams& p, const int32_t* links, int64_t
 
 }  // namespace lbm
 
+// Declarations for translation units that call the launchers but must not
+// instantiate the kernels themselves (they are built once per storage TU).
+#define LBM_EXTERN_STORAGE(ST)                                                                        \
+  namespace lbm {                                                                                     \
+  extern template int launch_stream_only<ST>(const FusedParams&, float*, cudaStream_t);               \
+  extern template int launch_fused_sc<ST>(const FusedParams&, cudaStream_t);                          \
+  extern template int launch_fused_persistent<ST>(const FusedParams&, int, int, int32_t*, cudaStream_t);             \
+  extern template int launch_convert<ST>(const FusedParams&, const float*, void*, int, cudaStream_t);  \
+  extern template int launch_reduce<ST>(const FusedParams&, double*, double*, cudaStream_t);          \
+  extern template int launch_momentum_exchange<ST>(const FusedParams&, const int32_t*, int64_t,       \
+                                                   double*, cudaStream_t);                            \
+  }
+
 #define LBM_INSTANTIATE_STORAGE(ST, VA, VB)                                                    \
   namespace lbm {                                                                               \
   template <>                                                                                   \
@@ -66,6 +195,8 @@ int launch_momentum_exchange(const FusedParams& p, const int32_t* links, int64_t
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "nodes_per_thread %d not built for this storage", V); \
   }                                                                                             \
   template int launch_stream_only<ST>(const FusedParams&, float*, cudaStream_t);                \
+  template int launch_fused_sc<ST>(const FusedParams&, cudaStream_t);                            \
+  template int launch_fused_persistent<ST>(const FusedParams&, int, int, int32_t*, cudaStream_t);              \
   template int launch_convert<ST>(const FusedParams&, const float*, void*, int, cudaStream_t);  \
   template int launch_reduce<ST>(const FusedParams&, double*, double*, cudaStream_t);           \
   template int launch_momentum_exchange<ST>(const FusedParams&, const int32_t*, int64_t, double*, \

@@ -5,6 +5,10 @@
 
 #include "lbm_fused_launch.cuh"
 
+LBM_EXTERN_STORAGE(LBM_STORE_F32)
+LBM_EXTERN_STORAGE(LBM_STORE_F16S)
+LBM_EXTERN_STORAGE(LBM_STORE_BF16S)
+
 struct LbmPlan {
   LbmPlanDesc d;
   LbmPlanBuffers b;
@@ -31,10 +35,27 @@ FusedParams params_for(LbmPlan* pl) {
   p.code = pl->b.code;
   p.seg_flags = pl->b.seg_flags;
   p.tau = pl->b.tau;
+  p.special = pl->d.pipeline == LBM_PIPE_DIRECT && !pl->d.sc ? pl->b.special : nullptr;
+  p.nspecial = p.special ? pl->b.nspecial : 0;
   return p;
 }
 
-int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s) {
+int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, int pipeline = LBM_PIPE_DIRECT,
+                   int32_t* status = nullptr, int tune = 0) {
+  if (p.sc) {
+    switch (st) {
+      case LBM_STORE_F32: return lbm::launch_fused_sc<LBM_STORE_F32>(p, s);
+      case LBM_STORE_F16S: return lbm::launch_fused_sc<LBM_STORE_F16S>(p, s);
+      default: return lbm::launch_fused_sc<LBM_STORE_BF16S>(p, s);
+    }
+  }
+  if (pipeline == LBM_PIPE_ASYNC || pipeline == LBM_PIPE_PREFETCH) {
+    switch (st) {
+      case LBM_STORE_F32: return lbm::launch_fused_persistent<LBM_STORE_F32>(p, pipeline, tune, status, s);
+      case LBM_STORE_F16S: return lbm::launch_fused_persistent<LBM_STORE_F16S>(p, pipeline, tune, status, s);
+      default: return lbm::launch_fused_persistent<LBM_STORE_BF16S>(p, pipeline, tune, status, s);
+    }
+  }
   switch (st) {
     case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, V, s);
     case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, V, s);
@@ -60,6 +81,21 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   const int V = d->nodes_per_thread;
   const bool vok = d->storage == LBM_STORE_F32 ? (V == 2 || V == 4) : (V == 4 || V == 8);
   if (!vok) return lbm_err::set(LBM_ERR_UNSUPPORTED, "nodes_per_thread %d for storage %d", V, d->storage);
+  if (d->pipeline < LBM_PIPE_DIRECT || d->pipeline > LBM_PIPE_PREFETCH)
+    return lbm_err::set(LBM_ERR_ARG, "pipeline %d", d->pipeline);
+  if (d->pipeline != LBM_PIPE_DIRECT && V != lbm::AV)
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "persistent pipelines run %d nodes per thread", lbm::AV);
+  if (d->pipeline == LBM_PIPE_ASYNC && (d->tune < 0 || d->tune >= LBM_ASYNC_TUNINGS))
+    return lbm_err::set(LBM_ERR_ARG, "async tuning %d", d->tune);
+  if (d->sc) {
+    if (d->pipeline != LBM_PIPE_DIRECT || V != lbm::AV)
+      return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans run the direct pipeline, %d nodes per thread",
+                          lbm::AV);
+    if (d->fluid_model != LBM_NEWTONIAN || d->nbc != 0)
+      return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans take no power law and no rewrite boundaries");
+    if (d->ny % lbm::SC_ROWS)
+      return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans need ny divisible by %d", lbm::SC_ROWS);
+  }
   if (d->nbc < 0 || d->nbc > LBM_MAX_BC) return lbm_err::set(LBM_ERR_ARG, "nbc %d", d->nbc);
   if (d->nprog < 0 || d->nprog > LBM_MAX_PROG) return lbm_err::set(LBM_ERR_ARG, "nprog %d", d->nprog);
   for (int i = 0; i < d->nbc; ++i) {
@@ -100,6 +136,14 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   p.nbc = d->nbc;
   std::memcpy(p.bc, d->bc, sizeof(p.bc));
   std::memcpy(p.prog, d->prog, sizeof(p.prog));
+  p.sc = d->sc;
+  p.g_coh = d->g_coh;
+  p.sc_T = d->sc_T;
+  p.eos = d->eos;
+  if (!(d->rho_ref >= 0.0f && d->rho_ref < 1e30f))
+    return lbm_err::set(LBM_ERR_ARG, "rho_ref %g must be finite and >= 0", (double)d->rho_ref);
+  const float rho_ref = d->rho_ref != 0.0f ? d->rho_ref : 1.0f;
+  for (int k = 0; k < 9; ++k) p.wsh[k] = d->storage == LBM_STORE_F32 ? 0.0f : lbm::W(k) * rho_ref;
   *out = pl;
   return LBM_OK;
 }
@@ -114,6 +158,13 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
   const size_t va = (size_t)storage_bytes(pl->d.storage) * pl->d.nodes_per_thread;
   if (!aligned(b->fa, va) || !aligned(b->fb, va) || !aligned(b->code, 16) || (b->tau && !aligned(b->tau, 16)))
     return lbm_err::set(LBM_ERR_ARG, "plan_bind: buffers must be 16-byte aligned");
+  if (pl->d.pipeline == LBM_PIPE_ASYNC && (!b->status || !aligned(b->fa, 16) || !aligned(b->fb, 16)))
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: the async pipeline needs a status word and 16-byte "
+                                     "aligned population buffers");
+  if (b->nspecial < 0 || (b->nspecial > 0 && !b->special) ||
+      (int64_t)b->nspecial > (int64_t)pl->d.ny * pl->base.nseg)
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d special segments for a %d x %d segment grid", b->nspecial,
+                        pl->d.ny, pl->base.nseg);
   pl->b = *b;
   pl->bound = true;
   pl->parity = 0;
@@ -125,7 +176,8 @@ int lbm_plan_run(LbmPlan* pl, int32_t nsteps, void* stream) {
   if (nsteps < 0) return lbm_err::set(LBM_ERR_ARG, "plan_run: nsteps %d", nsteps);
   for (int32_t s = 0; s < nsteps; ++s) {
     FusedParams p = params_for(pl);
-    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, (cudaStream_t)stream);
+    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, (cudaStream_t)stream,
+                            pl->d.pipeline, pl->b.status, pl->d.tune);
     if (rc) return rc;
     pl->parity ^= 1;
   }
@@ -212,7 +264,8 @@ int lbm_plan_run_monitored(LbmPlan* pl, int32_t nsteps, const int32_t* links, in
   cudaStream_t s = (cudaStream_t)stream;
   for (int32_t st = 0; st < nsteps; ++st) {
     FusedParams p = params_for(pl);
-    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, s);
+    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, s, pl->d.pipeline, pl->b.status,
+                            pl->d.tune);
     if (rc) return rc;
     pl->parity ^= 1;
     rc = mex(pl, links, n, series + 2 * (size_t)st, s);
@@ -282,7 +335,7 @@ __global__ void __launch_bounds__(lbm::REDUCE_TPB) k_reduce_chunked(const FusedP
     if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double v = S::dec64(src[(size_t)k * p.plane + q], lbm::W(k));
+      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
       a0 += v;
       if (lbm::CX(k)) a1 += lbm::CX(k) * v;
       if (lbm::CY(k)) a2 += lbm::CY(k) * v;

@@ -63,12 +63,19 @@ class LbmPlanDesc(ctypes.Structure):
                 ("pl_m", ctypes.c_float), ("pl_n", ctypes.c_float),
                 ("mrt_s", ctypes.c_float * 9), ("gravity", ctypes.c_float * 2),
                 ("nbc", ctypes.c_int32), ("bc", LbmBoundary * MAX_BC),
-                ("nprog", ctypes.c_int32), ("prog", (ctypes.c_int8 * PROG_LEN) * MAX_PROG)]
+                ("nprog", ctypes.c_int32), ("prog", (ctypes.c_int8 * PROG_LEN) * MAX_PROG),
+                ("pipeline", ctypes.c_int32), ("tune", ctypes.c_int32),
+                ("sc", ctypes.c_int32), ("g_coh", ctypes.c_float), ("sc_T", ctypes.c_float),
+                ("eos", LbmEos), ("rho_ref", ctypes.c_float)]
+
+
+PIPE_DIRECT, PIPE_ASYNC, PIPE_PREFETCH = 0, 1, 2
+ASYNC_TUNINGS = 4
 
 
 class LbmPlanBuffers(ctypes.Structure):
     _fields_ = [(n, _vp) for n in ("fa", "fb", "mom_a", "mom_b", "code", "seg_flags", "bc_vel",
-                                   "tau")]
+                                   "tau", "status", "special")] + [("nspecial", ctypes.c_int32)]
 
 
 class LbmError(RuntimeError):

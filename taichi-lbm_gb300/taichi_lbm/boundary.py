@@ -5,7 +5,8 @@ runs on the host: a geometry predicate is evaluated over the whole index box
 (vectorised over numpy index arrays when the predicate allows it, node by node
 otherwise) and the selected nodes are uploaded as an int32 (i, j) list.  The
 reference appends nodes with an atomic counter, so its order is arbitrary;
-here nodes are in row-major (i, then j) order.  Every per-step operation is a
+here nodes are in memory order (j, then i) so that per-group kernels read
+and write consecutive addresses.  Every per-step operation is a
 CUDA kernel launched through the C ABI.
 """
 import ctypes
@@ -139,7 +140,9 @@ class BoundaryClassifier:
     def get_group(self, spec):
         sel = evaluate_predicate(spec.geometry_fn, self.shape[0], self.shape[1], self.offset[0],
                                  self.offset[1], spec.vectorized)
-        nodes = np.argwhere(sel).astype(np.int32) + np.asarray(self.offset, np.int32)
+        # memory order (j, then i): consecutive group entries are consecutive
+        # addresses, so the per-group kernels' accesses coalesce
+        nodes = np.argwhere(sel.T)[:, ::-1].astype(np.int32) + np.asarray(self.offset, np.int32)
         dev = self.device
         if dev is None:
             dev = torch.device("cuda", torch.cuda.current_device())

@@ -20,6 +20,7 @@ class Pseudopotential:
     def __init__(self, params):
         p = {"a": None, "b": None, "R": 1.0, "G": 1.0}
         p.update(params)
+        self.params = dict(params)
         self.a, self.b, self.R, self.G = p["a"], p["b"], p["R"], p["G"]
         self.rho_cr = params["rho_cr"]
         self.pressure_cr = params["pressure_cr"]

@@ -27,7 +27,8 @@ from .collision import BGKCollision, MRTCollision, PowerLawFluid, TRTCollision
 from .lbm import stream_handle
 
 STORAGE = {"fp32": A.STORE_F32, "fp16s": A.STORE_F16S, "bf16s": A.STORE_BF16S}
-DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 8, A.STORE_BF16S: 8}
+DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 4, A.STORE_BF16S: 4}
+PIPELINE = {"direct": A.PIPE_DIRECT, "async": A.PIPE_ASYNC, "prefetch": A.PIPE_PREFETCH}
 
 
 def boundary_items(boundary_engine):
@@ -45,15 +46,35 @@ def boundary_items(boundary_engine):
 
 class FusedSolver:
     def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
-                 nodes_per_thread=None, local_relaxation=None):
-        if lb_field.sc_field is not None:
-            raise UnsupportedComposition("Shan-Chen lattices use the per-stage kernels in this build")
+                 nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
+                 sc_boundary_engine=None, two_pass=True, rho_ref=None):
+        self.sc = lb_field.sc_field
+        self.two_pass = bool(two_pass)
+        self.rho_ref = rho_ref
+        self.bsc = sc_boundary_engine
+        if self.sc is not None:
+            from .shanchen import PeriodicPsi_BT, PeriodicPsi_LR, ShanChenForceC1
+            if not isinstance(self.sc, ShanChenForceC1):
+                raise UnsupportedComposition("the fused Shan-Chen step is single-component")
+            kinds = {type(b) for b in (sc_boundary_engine.boundary_conditions.values()
+                                       if sc_boundary_engine is not None else [])}
+            if kinds != {PeriodicPsi_LR, PeriodicPsi_BT}:
+                raise UnsupportedComposition("the fused Shan-Chen step needs the psi boundaries "
+                                             "PeriodicPsi_LR and PeriodicPsi_BT (a periodic lattice)")
+            if pipeline != "direct" or lb_field.NY % 8:
+                raise UnsupportedComposition("the fused Shan-Chen step runs the direct pipeline on "
+                                             "lattices with NY divisible by 8")
         self.lb = lb_field
         self.me = macroscopic_engine
         self.coll = collision
         self.be = boundary_engine
         self.storage = STORAGE[storage] if isinstance(storage, str) else int(storage)
+        self.pipeline = PIPELINE[pipeline] if isinstance(pipeline, str) else int(pipeline)
         self.V = int(nodes_per_thread or DEFAULT_V[self.storage])
+        self.tune = int(tune)
+        if self.pipeline != A.PIPE_DIRECT:
+            self.V = 4
+        self.status = torch.zeros(1, dtype=torch.int32, device=lb_field.device)
         if local_relaxation is None:
             local_relaxation = isinstance(collision.fluid_model, PowerLawFluid)
         self.powerlaw = bool(local_relaxation)
@@ -68,6 +89,17 @@ class FusedSolver:
         self._build()
 
     # ------------------------------------------------------------ build
+    def _rho_ref(self):
+        """Reference density of the 16-bit storage shift: the mean density of
+        the collision group at plan build (1 when the lattice holds none yet)."""
+        if self.rho_ref is not None:
+            return float(self.rho_ref)
+        nd = torch.as_tensor(self.group.nodes, device=self.lb._rho.device).long()
+        if nd.numel() == 0:
+            return 1.0
+        r = float(self.lb._rho[nd[:, 1], nd[:, 0]].double().mean().item())
+        return r if np.isfinite(r) and r > 0.0 else 1.0
+
     def _uniform(self, field_tensor, planes=None):
         nd = torch.as_tensor(self.group.nodes, device=field_tensor.device).long()
         if planes is None:
@@ -95,6 +127,8 @@ class FusedSolver:
         d.nx, d.ny, d.pitch = nx, ny, P
         d.storage = self.storage
         d.nodes_per_thread = self.V
+        d.pipeline = self.pipeline
+        d.tune = self.tune
         d.fluid_model = A.POWERLAW if self.powerlaw else A.NEWTONIAN
         d.tau_min, d.tau_max = float(c.tau_min), float(c.tau_max)
         if self.powerlaw:
@@ -126,6 +160,16 @@ class FusedSolver:
             raise UnsupportedComposition(f"unknown collision {type(c).__name__}")
         g = np.asarray(lb.gravity_force, np.float32).reshape(2)
         d.gravity[0], d.gravity[1] = float(g[0]), float(g[1])
+        if self.sc is not None:
+            if cp.instances or not (cp.code == A.CODE_ACTIVE).all():
+                raise UnsupportedComposition("the fused Shan-Chen step needs every node colliding and "
+                                             "streaming periodically, with no rewrite boundaries")
+            if self.powerlaw:
+                raise UnsupportedComposition("the fused Shan-Chen step is Newtonian")
+            d.sc = 1
+            d.g_coh = float(self.sc.g_coh)
+            d.sc_T = self._uniform(lb._T)
+            d.eos = self.sc.psi.struct()
 
         # device-side plan data
         self.code = torch.zeros((ny, P), dtype=torch.int16, device=dev)
@@ -147,7 +191,12 @@ class FusedSolver:
         for p in range(A.MAX_PROG):
             for s in range(A.PROG_LEN):
                 d.prog[p][s] = int(cp.programs[p, s])
+        d.rho_ref = self._rho_ref()
         self.desc = d
+        # flagged segments, listed for the two-pass direct step
+        flagged = np.flatnonzero(np.asarray(cp.seg_flags).ravel()).astype(np.int32)
+        self.special = torch.as_tensor(flagged if flagged.size else np.zeros(1, np.int32), device=dev)
+        self.nspecial = int(flagged.size)
         self.mom = [torch.zeros((3, ny, P), dtype=torch.float32, device=dev) for _ in range(2)]
         if self.storage == A.STORE_F32:
             self.fbuf = None
@@ -179,14 +228,26 @@ class FusedSolver:
         b.seg_flags = self.seg_flags.data_ptr()
         b.bc_vel = None if self.bc_vel is None else self.bc_vel.data_ptr()
         b.tau = self.tau_state.data_ptr() if self.powerlaw else None
+        b.status = self.status.data_ptr()
+        if self.two_pass and self.pipeline == A.PIPE_DIRECT:
+            b.special, b.nspecial = self.special.data_ptr(), self.nspecial
         A.call("lbm_plan_bind", self._plan, ctypes.byref(b))
 
-    def _staged_first_step(self):
-        lb, me, c = self.lb, self.me, self.coll
+    def _moments(self):
+        """The moment stages of a step (with the Shan-Chen force when present)."""
+        lb, me = self.lb, self.me
         me.density(lb)
         me.pressure(lb)
+        if self.sc is not None:
+            self.sc.update_psi(lb)
+            self.bsc.apply_boundary_conditions(lb)
+            self.sc.cau_SCforce(lb)
         me.force_density(lb)
         me.velocity(lb)
+
+    def _staged_first_step(self):
+        lb, c = self.lb, self.coll
+        self._moments()
         if self.powerlaw:
             c.shear_rate(lb)
             c.relaxation_time(lb)
@@ -214,6 +275,10 @@ class FusedSolver:
         lb = self.lb
         lb._fused_owner = None
         self._live = False
+        if self.pipeline == A.PIPE_ASYNC and int(self.status.item()) != 0:
+            self.status.zero_()
+            raise A.LbmError("fused step: a wait on a shared-memory copy exceeded its time budget; "
+                             "the state is invalid")
         par = ctypes.c_int32()
         A.call("lbm_plan_get_parity", self._plan, ctypes.byref(par))
         s = stream_handle()
@@ -234,11 +299,7 @@ class FusedSolver:
                 c._tau_antisym[nd[:, 1], nd[:, 0]] = float(c.magic[0]) / (ts - 0.5) + 0.5
             elif isinstance(c, MRTCollision):
                 c._diag[8].copy_(c._diag[7])
-        me = self.me
-        me.density(lb)
-        me.pressure(lb)
-        me.force_density(lb)
-        me.velocity(lb)
+        self._moments()
 
     def sync(self):
         if getattr(self, "_live", False):
@@ -274,6 +335,8 @@ class FusedSolver:
         elif n > 1:
             self.run(n - 1)
         self.finish()
+        if self.sc is not None:  # the Shan-Chen driver advances LBField.time (lbm.py:150-151)
+            self.lb.time[None] = self.lb.time[None] + n
         return series
 
     def solid_links(self):

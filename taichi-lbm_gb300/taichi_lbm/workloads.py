@@ -85,3 +85,50 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
     lb.vel.fill([0.0, 0.0])
     lb.init_LBM(coll, fluid.group)
     return lb, me, coll, be
+
+
+def carnahan_starling(tl, T_over_Tc, a=1.0, b=4.0, R=1.0, G=-1.0):
+    """CS_psi with a, b, R and the temperature T = (T/Tc) Tc, Tc = 0.3773 a / (b R)."""
+    Tc = 0.3773 * a / (b * R)
+    psi = tl.CS_psi({"a": a, "b": b, "R": R, "G": G, "rho_cr": 0.1304 / b * 4.0,
+                     "pressure_cr": 0.0707 * a / b ** 2, "temperature_cr": Tc})
+    return psi, T_over_Tc * Tc
+
+
+def shan_chen_box(tl, nx, ny, psi, g_coh, T, rho_init, model="bgk", tau=1.0, magic=0.25,
+                  name="shan_chen", keep_init=True):
+    """Fully periodic single-component Shan-Chen lattice (the reference's
+    two-phase separation case, cases/Bubble or two-phase separation.py):
+    periodic stream carrier, PeriodicPsi_LR + PeriodicPsi_BT, uniform T,
+    initial density rho_init (NX, NY), u = 0."""
+    lb = tl.LBField(name, nx, ny, 1)
+    lb.keep_init_snapshot = keep_init
+    be = tl.BoundaryEngine()
+    cls = tl.BoundaryClassifier((nx, ny))
+    mask = lb.mask.arr
+
+    def fluid_fn(i, j):
+        return mask[i, j] == 1
+
+    fluid = tl.FluidBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    fluid.precompute(classifier=cls)
+    be.add_boundary_condition("fluid", fluid)
+    per = tl.PeriodicAllBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    per.precompute(classifier=cls)
+    be.add_boundary_condition("stream", per)
+    lb.neighbor_classify()
+    me = tl.MacroscopicEngine(fluid.group)
+    nu = (tau - 0.5) / 3.0
+    params = {"group": fluid.group, "fluid_model": tl.NewtonianFluid(nu=nu), "NX": nx, "NY": ny,
+              "num_components": 1, "shearviscosity": [nu], "magic": [magic], "bulkviscosity": [nu]}
+    coll = {"bgk": tl.BGKCollision, "trt": tl.TRTCollision, "mrt": tl.MRTCollision}[model](params)
+    sc = tl.ShanChenForceC1({"lb_field": lb, "g_coh": g_coh, "group": fluid.group, "psi": psi})
+    lb.sc_field = sc
+    bsc = tl.BoundaryEngineSC()
+    bsc.add_boundary_condition("periodicLR", tl.PeriodicPsi_LR())
+    bsc.add_boundary_condition("periodicBT", tl.PeriodicPsi_BT())
+    lb.T.fill(float(T))
+    lb.rho.from_numpy(np.asarray(rho_init, np.float32).reshape(nx, ny, 1))
+    lb.vel.fill([0.0, 0.0])
+    lb.init_LBM(coll, fluid.group)
+    return lb, me, coll, be, sc, bsc

@@ -236,4 +236,12 @@ def describe(lb, coll, be, steps, step_kind="standard", fp="f32"):
         if nd.size:
             c["mrt_diag"] = [float(v) for v in coll._diag[:, nd[0, 1], nd[0, 0]].cpu().numpy()]
     meta["collision"] = c
+    sc = lb.sc_field
+    if sc is not None:
+        kind = {0: "sc", 1: "vdw", 2: "rk", 3: "pr", 4: "cs"}[sc.psi.kind]
+        meta["sc"] = {"g_coh": float(sc.g_coh),
+                      "psi": ["sc", float(sc.psi.rho0)] if kind == "sc" else [kind, sc.psi.params]}
+        meta["psi_bcs"] = ["periodic_lr", "periodic_bt"]
+        meta["step_kind"] = "shanchen"
+        arrays["T"] = T0
     return meta, arrays

@@ -62,11 +62,12 @@ def test_staged_matches_reference_fixture(tl, name):
     check_parity(got, arrays, fp64_solution(meta, arrays), keys, tol_for(meta))
 
 
+@pytest.mark.parametrize("pipeline", ["direct", "async", "prefetch"])
 @pytest.mark.parametrize("name", sorted(set(fixture_names()) - F64_CASES - SC_CASES))
-def test_fused_matches_reference_fixture(tl, name):
+def test_fused_matches_reference_fixture(tl, name, pipeline):
     meta, arrays = load_fixture(name)
     lb, me, coll, be, sc, bsc = build_from_case(tl, meta, arrays)
-    solver = tl.FusedSolver(lb, me, coll, be)
+    solver = tl.FusedSolver(lb, me, coll, be, pipeline=pipeline)
     solver.step(meta["steps"])
     torch.cuda.synchronize()
     check_parity(fields_of(lb), arrays, fp64_solution(meta, arrays), ("f", "f2", "rho", "vel"),
@@ -83,9 +84,10 @@ def test_value_fn_inlet_equals_per_node_boundaries(tl):
     check_parity(fields_of(lb), arrays, fp64_solution(meta, arrays), ("f", "rho", "vel"), TOL)
 
 
+@pytest.mark.parametrize("pipeline", ["direct", "async", "prefetch"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
 @pytest.mark.parametrize("shape", [(256, 64), (301, 67)])
-def test_fused_matches_oracle_cylinder(tl, model, shape):
+def test_fused_matches_oracle_cylinder(tl, model, shape, pipeline):
     """Larger lattices (one odd width exercises the row-end wrap) against the
     oracle: 200 steps."""
     nx, ny = shape
@@ -93,15 +95,17 @@ def test_fused_matches_oracle_cylinder(tl, model, shape):
     lb, me, coll, be = cylinder_channel(tl, nx, ny, ny / 10, nx / 5, ny / 2 - 0.5, 0.56, 0.05,
                                         model=model, mrt_s=s)
     meta, arrays = describe(lb, coll, be, 200)
-    tl.FusedSolver(lb, me, coll, be).step(200)
+    tl.FusedSolver(lb, me, coll, be, pipeline=pipeline).step(200)
     check_parity(fields_of(lb), O.replay(meta, arrays), fp64_solution(meta, arrays),
                  ("f", "rho", "vel"), TOL)
 
 
-def test_fused_periodic_box_odd_width(tl):
+@pytest.mark.parametrize("pipeline", ["direct", "async", "prefetch"])
+@pytest.mark.parametrize("nx,ny", [(37, 23), (389, 9)])
+def test_fused_periodic_box_odd_width(tl, pipeline, nx, ny):
     """Fully periodic lattice whose width is not a multiple of the vector
-    width: every wrap-around path of the pull loads."""
-    nx, ny = 37, 23
+    width (and, at 389, spans several row segments): every wrap-around path
+    of the pull loads."""
     lb = tl.LBField("box", nx, ny, 1)
     lb.keep_init_snapshot = True
     cls = tl.BoundaryClassifier((nx, ny))
@@ -122,7 +126,7 @@ def test_fused_periodic_box_odd_width(tl):
     lb.set_gravity([1e-5, -2e-5])
     lb.init_LBM(coll, fl.group)
     meta, arrays = describe(lb, coll, be, 150)
-    tl.FusedSolver(lb, me, coll, be).step(150)
+    tl.FusedSolver(lb, me, coll, be, pipeline=pipeline).step(150)
     check_parity(fields_of(lb), O.replay(meta, arrays), fp64_solution(meta, arrays),
                  ("f", "rho", "vel"), TOL)
 
@@ -146,13 +150,14 @@ def test_fused_equals_staged_and_run_is_resumable(tl):
         assert rel_err(runs[1][k], runs[2][k]) < TOL, k
 
 
+@pytest.mark.parametrize("pipeline", ["direct", "async", "prefetch"])
 @pytest.mark.parametrize("storage,tol", [("fp16s", 2e-3), ("bf16s", 2e-2)])
-def test_shifted_storage_against_fp64_oracle(tl, storage, tol):
+def test_shifted_storage_against_fp64_oracle(tl, storage, tol, pipeline):
     nx, ny = 256, 64
     lb, me, coll, be = cylinder_channel(tl, nx, ny, 6.4, 51.2, 31.5, 0.6, 0.04, model="bgk")
     meta, arrays = describe(lb, coll, be, 300)
     meta["fp"] = "f64"
-    tl.FusedSolver(lb, me, coll, be, storage=storage).step(300)
+    tl.FusedSolver(lb, me, coll, be, storage=storage, pipeline=pipeline).step(300)
     ref = O.replay(meta, arrays)
     got = fields_of(lb)
     assert rel_err(got["rho"], ref["rho"]) < tol
@@ -199,3 +204,27 @@ def test_drag_lift_series_matches_oracle(tl):
     ref = np.array(ref)
     assert np.abs(series - ref).max() / np.abs(ref).max() < 1e-4
     assert series[-1, 0] > 0  # drag points downstream
+
+
+@pytest.mark.parametrize("model,storage,tol", [("bgk", "fp32", TOL), ("mrt", "fp32", TOL),
+                                               ("trt", "fp32", TOL), ("bgk", "fp16s", 3e-3)])
+def test_fused_shan_chen_matches_oracle(tl, model, storage, tol):
+    """Fused Shan-Chen kernel (psi tile in shared memory) vs the oracle's
+    reference-order update_psi -> periodic psi -> cau_SCforce -> collide."""
+    from taichi_lbm.workloads import carnahan_starling, shan_chen_box
+    nx, ny = 200, 64  # two row segments, the second one partial
+    rng = np.random.Generator(np.random.PCG64(11))
+    psi, T = carnahan_starling(tl, 0.8)
+    rho0 = 0.25 * (1.0 + rng.uniform(-0.01, 0.01, size=(nx, ny)))
+    lb, me, coll, be, sc, bsc = shan_chen_box(tl, nx, ny, psi, -1.0, T, rho0, model=model)
+    meta, arrays = describe(lb, coll, be, 120)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, sc_boundary_engine=bsc)
+    solver.step(120)
+    got = fields_of(lb)
+    if storage == "fp32":
+        check_parity(got, O.replay(meta, arrays), fp64_solution(meta, arrays), ("f", "rho", "vel", "psi"),
+                     tol)
+    else:
+        ref = fp64_solution(meta, arrays)
+        assert rel_err(got["rho"], ref["rho"]) < tol
+    assert lb.time[None] == 120

@@ -23,7 +23,7 @@ def test_library_exports_every_header_function(built):
     for n in names:
         assert hasattr(lib, n), f"{n} declared in lbm_gb300.h but not exported"
     assert set(names) == set(_capi.EXPORTED)
-    assert lib.lbm_abi_version() == 1
+    assert lib.lbm_abi_version() == 2
 
 
 def test_library_reports_argument_errors(built):
@@ -59,7 +59,7 @@ def test_classifier_vectorised_equals_scalar():
     cls = BoundaryClassifier((20, 9), device=torch.device("cpu"))
     g = cls.get_group(BoundarySpec(geometry_fn=scalar))
     assert g.count[None] == a.sum()
-    assert np.array_equal(g.nodes, np.argwhere(a))
+    assert np.array_equal(g.nodes, np.argwhere(a.T)[:, ::-1])  # row-major in memory: j, then i
     gp = BoundaryClassifier((22, 11), offset=(-1, -1), device=torch.device("cpu")).get_group(
         BoundarySpec(geometry_fn=lambda i, j: (i == -1) | (j == 9)))
     assert gp.nodes[:, 0].min() == -1 and gp.count[None] == 11 + 22 - 1
