@@ -289,14 +289,17 @@ def run_ours(a):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes_per_launch": BYTES_PER_LU[a.storage] * active,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": ("one fused step: k_fused_bulk (plain segments) + k_fused_special "
+                                "(flagged segments), timed together"
+                                if solver.launches_per_step == 2 else "one fused step (one launch)")},
         "clocks": clocks,
         "e2e": {"value": round(active * K * ws / e2e_dt / 1e6, 1), "unit": METRIC,
                 "h2d_bytes_per_step": round(h2d / K, 1), "d2h_bytes_per_step": round(d2h / K, 1),
                 "seconds": round(e2e_dt, 4),
                 "what": "upload rho/u from pinned host memory, init_LBM, FusedSolver.step(K), "
                         "download rho/u (the inputs and result are per run; bytes are per step)"},
-        "gpu_launches": K,
+        "gpu_launches": K * solver.launches_per_step,
     }
     del solver, lb, me, coll, be
     torch.cuda.empty_cache()

@@ -278,6 +278,11 @@ typedef struct LbmPlanBuffers {
    * the listed segments; NULL keeps one general launch per step.          */
   const int32_t* special;
   int32_t nspecial;
+  /* with a special list: 1 = run the listed segments on a plan-owned
+   * high-priority stream, forked from the caller's stream by an event before
+   * the plain segments are launched and joined back after them, so the two
+   * kernels overlap; 0 = both on the caller's stream, one after the other */
+  int32_t special_stream;
 } LbmPlanBuffers;
 
 typedef struct LbmPlan LbmPlan;

@@ -54,6 +54,8 @@ struct FusedParams {
   // 16-bit storage holds f_k - wsh[k], wsh[k] = w_k * rho_ref (the plan's
   // reference density); fp32 storage ignores it
   float wsh[9];
+  float rho_shift;  // sum_k wsh[k]
+  float mwsh[9];    // MRT moments of the shift, M wsh
 };
 
 // ------------------------------------------------------------ storage
@@ -328,27 +330,8 @@ __global__ void __launch_bounds__(256) k_fused(const FusedParams p) {
   fused_tail<MODEL, PL, ST, V>(p, f, y, seg, x0, x0 < p.nx);
 }
 
-// Two-pass form of the same step.  k_fused_bulk takes the plain segments
-// (seg_flags == 0: every node collides and streams all nine links, no
-// boundary program, no saved moments), with the body force fixed at compile
-// time, and leaves the flagged segments to k_fused_special, which walks the
-// compact list p.special of their indices (y * nseg + seg).  The two write
-// disjoint nodes and read only the source state, so their order within a
-// step is free.
-template <int MODEL, bool PL, int ST, int V, int FORCE>
-__global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
-  const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= (long long)p.ny * p.nseg) return;
-  if (p.seg_flags[warp]) return;  // uniform over the warp
-  const int y = (int)(warp / p.nseg);
-  const int seg = (int)(warp - (long long)y * p.nseg);
-  const int x0 = seg * 32 * V + lane * V;
-  float f[V][9];
-  gather_direct<ST, V>(p, y, seg, lane, f);
-  fused_tail<MODEL, PL, ST, V, false, FORCE>(p, f, y, seg, x0, x0 < p.nx);
-}
-
+// General kernel of the two-pass direct step (the lean one is k_fused_bulk,
+// lbm_fused_lean.cuh): the flagged segments listed in p.special.
 template <int MODEL, bool PL, int ST, int V>
 __global__ void __launch_bounds__(256) k_fused_special(const FusedParams p) {
   const int lane = threadIdx.x & 31;

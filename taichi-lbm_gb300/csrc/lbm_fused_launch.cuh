@@ -4,6 +4,7 @@
 
 #include "lbm_fused.cuh"
 #include "lbm_fused_async.cuh"
+#include "lbm_fused_lean.cuh"
 #include "lbm_fused_sc.cuh"
 
 namespace lbm {
@@ -100,30 +101,34 @@ int launch_fused_persistent(const FusedParams& p, int pipeline, int tune, int32_
   }
 }
 
-// plain segments with a compile-time force switch, then the listed ones
+// The listed (flagged) segments on stream s2, then the plain segments, with
+// a compile-time force switch, on s.  s2 == s serialises the two; a caller
+// passing another stream has forked it from s and joins it back after.
 template <int MODEL, bool PL, int ST, int V>
-int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s) {
+int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s, cudaStream_t s2) {
+  if (p.nspecial > 0) {
+    k_fused_special<MODEL, PL, ST, V><<<(unsigned)((p.nspecial + 7) / 8), 256, 0, s2>>>(p);
+    int rc = lbm_err::launch("fused step (flagged segments)");
+    if (rc) return rc;
+  }
   if (p.has_force) k_fused_bulk<MODEL, PL, ST, V, 1><<<blocks, 256, 0, s>>>(p);
   else k_fused_bulk<MODEL, PL, ST, V, 0><<<blocks, 256, 0, s>>>(p);
-  int rc = lbm_err::launch("fused step (plain segments)");
-  if (rc || p.nspecial == 0) return rc;
-  k_fused_special<MODEL, PL, ST, V><<<(unsigned)((p.nspecial + 7) / 8), 256, 0, s>>>(p);
-  return lbm_err::launch("fused step (flagged segments)");
+  return lbm_err::launch("fused step (plain segments)");
 }
 
 template <int ST, int V>
-int launch_fused_v(const FusedParams& p, cudaStream_t s) {
+int launch_fused_v(const FusedParams& p, cudaStream_t s, cudaStream_t s2) {
   const long long warps = (long long)p.ny * p.nseg;
   const unsigned blocks = (unsigned)((warps + 7) / 8);
   const bool pl = p.fluid_model == LBM_POWERLAW;
   if (p.special) {
     switch (p.model * 2 + (pl ? 1 : 0)) {
-      case 0: return launch_two_pass<LBM_BGK, false, ST, V>(p, blocks, s);
-      case 1: return launch_two_pass<LBM_BGK, true, ST, V>(p, blocks, s);
-      case 2: return launch_two_pass<LBM_TRT, false, ST, V>(p, blocks, s);
-      case 3: return launch_two_pass<LBM_TRT, true, ST, V>(p, blocks, s);
-      case 4: return launch_two_pass<LBM_MRT, false, ST, V>(p, blocks, s);
-      case 5: return launch_two_pass<LBM_MRT, true, ST, V>(p, blocks, s);
+      case 0: return launch_two_pass<LBM_BGK, false, ST, V>(p, blocks, s, s2);
+      case 1: return launch_two_pass<LBM_BGK, true, ST, V>(p, blocks, s, s2);
+      case 2: return launch_two_pass<LBM_TRT, false, ST, V>(p, blocks, s, s2);
+      case 3: return launch_two_pass<LBM_TRT, true, ST, V>(p, blocks, s, s2);
+      case 4: return launch_two_pass<LBM_MRT, false, ST, V>(p, blocks, s, s2);
+      case 5: return launch_two_pass<LBM_MRT, true, ST, V>(p, blocks, s, s2);
       default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
     }
   }
@@ -142,7 +147,7 @@ int launch_fused_v(const FusedParams& p, cudaStream_t s) {
 }
 
 template <int ST>
-int launch_fused(const FusedParams& p, int V, cudaStream_t s);
+int launch_fused(const FusedParams& p, int V, cudaStream_t s, cudaStream_t s2);
 
 template <int ST>
 int launch_stream_only(const FusedParams& p, float* out, cudaStream_t s) {
@@ -189,9 +194,9 @@ int launch_momentum_exchange(const FusedParams& p, const int32_t* links, int64_t
 #define LBM_INSTANTIATE_STORAGE(ST, VA, VB)                                                    \
   namespace lbm {                                                                               \
   template <>                                                                                   \
-  int launch_fused<ST>(const FusedParams& p, int V, cudaStream_t s) {                           \
-    if (V == VA) return launch_fused_v<ST, VA>(p, s);                                           \
-    if (V == VB) return launch_fused_v<ST, VB>(p, s);                                           \
+  int launch_fused<ST>(const FusedParams& p, int V, cudaStream_t s, cudaStream_t s2) {          \
+    if (V == VA) return launch_fused_v<ST, VA>(p, s, s2);                                       \
+    if (V == VB) return launch_fused_v<ST, VB>(p, s, s2);                                       \
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "nodes_per_thread %d not built for this storage", V); \
   }                                                                                             \
   template int launch_stream_only<ST>(const FusedParams&, float*, cudaStream_t);                \

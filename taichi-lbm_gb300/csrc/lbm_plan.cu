@@ -15,6 +15,11 @@ struct LbmPlan {
   bool bound = false;
   int parity = 0;
   lbm::FusedParams base;
+  // two-pass direct step: the flagged segments run on this plan-owned
+  // high-priority stream, forked from and joined back to the caller's stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int side_dev = -1;
 };
 
 namespace {
@@ -40,8 +45,8 @@ FusedParams params_for(LbmPlan* pl) {
   return p;
 }
 
-int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, int pipeline = LBM_PIPE_DIRECT,
-                   int32_t* status = nullptr, int tune = 0) {
+int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, cudaStream_t s2,
+                   int pipeline = LBM_PIPE_DIRECT, int32_t* status = nullptr, int tune = 0) {
   if (p.sc) {
     switch (st) {
       case LBM_STORE_F32: return lbm::launch_fused_sc<LBM_STORE_F32>(p, s);
@@ -57,10 +62,65 @@ int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, int pipe
     }
   }
   switch (st) {
-    case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, V, s);
-    case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, V, s);
-    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, V, s);
+    case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, V, s, s2);
+    case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, V, s, s2);
+    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, V, s, s2);
   }
+}
+
+void release_side(LbmPlan* pl) {
+  if (pl->fork) cudaEventDestroy(pl->fork);
+  if (pl->join) cudaEventDestroy(pl->join);
+  if (pl->side) cudaStreamDestroy(pl->side);
+  pl->fork = pl->join = nullptr;
+  pl->side = nullptr;
+  pl->side_dev = -1;
+}
+
+// the side stream and its two events on the current device
+int ensure_side(LbmPlan* pl) {
+  int dev = 0;
+  int rc = lbm_err::cuda(cudaGetDevice(&dev), "plan_run: device");
+  if (rc) return rc;
+  if (pl->side && pl->side_dev == dev) return LBM_OK;
+  release_side(pl);
+  int lo = 0, hi = 0;
+  rc = lbm_err::cuda(cudaDeviceGetStreamPriorityRange(&lo, &hi), "plan_run: stream priorities");
+  if (!rc) rc = lbm_err::cuda(cudaStreamCreateWithPriority(&pl->side, cudaStreamNonBlocking, hi),
+                              "plan_run: side stream");
+  if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming), "plan_run: event");
+  if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming), "plan_run: event");
+  if (rc) {
+    release_side(pl);
+    return rc;
+  }
+  pl->side_dev = dev;
+  return LBM_OK;
+}
+
+// one fused step on stream s and the parity flip
+int step_once(LbmPlan* pl, cudaStream_t s) {
+  FusedParams p = params_for(pl);
+  const bool fork = p.special && p.nspecial > 0 && pl->b.special_stream;
+  cudaStream_t s2 = s;
+  if (fork) {
+    int rc = ensure_side(pl);
+    if (rc) return rc;
+    s2 = pl->side;
+    rc = lbm_err::cuda(cudaEventRecord(pl->fork, s), "plan_run: fork");
+    if (!rc) rc = lbm_err::cuda(cudaStreamWaitEvent(s2, pl->fork, 0), "plan_run: fork");
+    if (rc) return rc;
+  }
+  int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, s, s2, pl->d.pipeline, pl->b.status,
+                          pl->d.tune);
+  if (fork) {  // join even after a failed launch, so s never runs ahead of s2
+    int rj = lbm_err::cuda(cudaEventRecord(pl->join, s2), "plan_run: join");
+    if (!rj) rj = lbm_err::cuda(cudaStreamWaitEvent(s, pl->join, 0), "plan_run: join");
+    if (!rc) rc = rj;
+  }
+  if (rc) return rc;
+  pl->parity ^= 1;
+  return LBM_OK;
 }
 
 }  // namespace
@@ -144,6 +204,14 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
     return lbm_err::set(LBM_ERR_ARG, "rho_ref %g must be finite and >= 0", (double)d->rho_ref);
   const float rho_ref = d->rho_ref != 0.0f ? d->rho_ref : 1.0f;
   for (int k = 0; k < 9; ++k) p.wsh[k] = d->storage == LBM_STORE_F32 ? 0.0f : lbm::W(k) * rho_ref;
+  double sum = 0.0;
+  for (int k = 0; k < 9; ++k) sum += p.wsh[k];
+  p.rho_shift = (float)sum;
+  for (int a = 0; a < 9; ++a) {
+    double m = 0.0;
+    for (int k = 0; k < 9; ++k) m += (double)lbm::MRT_M(a, k) * p.wsh[k];
+    p.mwsh[a] = (float)m;
+  }
   *out = pl;
   return LBM_OK;
 }
@@ -175,11 +243,8 @@ int lbm_plan_run(LbmPlan* pl, int32_t nsteps, void* stream) {
   if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "plan_run: plan not bound");
   if (nsteps < 0) return lbm_err::set(LBM_ERR_ARG, "plan_run: nsteps %d", nsteps);
   for (int32_t s = 0; s < nsteps; ++s) {
-    FusedParams p = params_for(pl);
-    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, (cudaStream_t)stream,
-                            pl->d.pipeline, pl->b.status, pl->d.tune);
+    int rc = step_once(pl, (cudaStream_t)stream);
     if (rc) return rc;
-    pl->parity ^= 1;
   }
   return LBM_OK;
 }
@@ -237,6 +302,7 @@ int lbm_plan_export(LbmPlan* pl, float* f_post, void* stream) {
 }
 
 int lbm_plan_destroy(LbmPlan* pl) {
+  if (pl) release_side(pl);
   delete pl;
   return LBM_OK;
 }
@@ -263,11 +329,8 @@ int lbm_plan_run_monitored(LbmPlan* pl, int32_t nsteps, const int32_t* links, in
     return lbm_err::set(LBM_ERR_ARG, "run_monitored: bad arguments");
   cudaStream_t s = (cudaStream_t)stream;
   for (int32_t st = 0; st < nsteps; ++st) {
-    FusedParams p = params_for(pl);
-    int rc = dispatch_fused(p, pl->d.storage, pl->d.nodes_per_thread, s, pl->d.pipeline, pl->b.status,
-                            pl->d.tune);
+    int rc = step_once(pl, s);
     if (rc) return rc;
-    pl->parity ^= 1;
     rc = mex(pl, links, n, series + 2 * (size_t)st, s);
     if (rc) return rc;
   }

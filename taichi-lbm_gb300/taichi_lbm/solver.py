@@ -47,9 +47,10 @@ def boundary_items(boundary_engine):
 class FusedSolver:
     def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
                  nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
-                 sc_boundary_engine=None, two_pass=True, rho_ref=None):
+                 sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True):
         self.sc = lb_field.sc_field
         self.two_pass = bool(two_pass)
+        self.overlap = bool(overlap)
         self.rho_ref = rho_ref
         self.bsc = sc_boundary_engine
         if self.sc is not None:
@@ -231,6 +232,7 @@ class FusedSolver:
         b.status = self.status.data_ptr()
         if self.two_pass and self.pipeline == A.PIPE_DIRECT:
             b.special, b.nspecial = self.special.data_ptr(), self.nspecial
+            b.special_stream = 1 if self.overlap else 0
         A.call("lbm_plan_bind", self._plan, ctypes.byref(b))
 
     def _moments(self):
@@ -266,8 +268,16 @@ class FusedSolver:
         lb._fused_owner = self
         self._live = True
 
+    @property
+    def launches_per_step(self):
+        """Kernel launches of one lbm_plan_run step: two for the two-pass
+        direct step (plain segments, then the listed ones), else one."""
+        if self.sc is None and self.pipeline == A.PIPE_DIRECT and self.two_pass and self.nspecial:
+            return 2
+        return 1
+
     def run(self, nsteps):
-        """nsteps fused launches on the current state (no staging)."""
+        """nsteps fused steps on the current state (no staging)."""
         A.call("lbm_plan_run", self._plan, int(nsteps), stream_handle())
 
     def finish(self):
