@@ -239,7 +239,11 @@ typedef struct LbmPlanDesc {
                            current one (nodes_per_thread == 4)             */
   int32_t tune;         /* LBM_PIPE_ASYNC: 0..LBM_ASYNC_TUNINGS-1 selects
                            (warps per block, stages per warp) =
-                           (8,2) (6,3) (4,4) (16,2)                         */
+                           (8,2) (6,3) (4,4) (16,2);
+                           LBM_PIPE_PREFETCH with a plain list:
+                           0..LBM_PREFETCH_TUNINGS-1 selects
+                           (8,2) (8,3) (4,4) (16,2) for the plain segments'
+                           shared-memory ring                               */
   /* Single-component Shan-Chen (ExternalForce.py:122-158) on a fully periodic
    * lattice: each step computes psi(rho, T) from the post-stream populations,
    * F = -g_coh psi(x) sum_k w_k c_k psi(x + c_k) + gravity, then collides.
@@ -257,6 +261,7 @@ typedef struct LbmPlanDesc {
 
 enum { LBM_PIPE_DIRECT = 0, LBM_PIPE_ASYNC = 1, LBM_PIPE_PREFETCH = 2 };
 #define LBM_ASYNC_TUNINGS 4
+#define LBM_PREFETCH_TUNINGS 4
 /* *status (LbmPlanBuffers.status) after an async step: 0, or 1 when a wait on
  * a copy exceeded its time budget (the step's output is then invalid). */
 
@@ -272,7 +277,7 @@ typedef struct LbmPlanBuffers {
   float* tau;           /* [ny][pitch] power-law state (BGK tau, TRT tau_sym,
                            MRT diag[7]) or NULL                              */
   int32_t* status;      /* one device int32 (LBM_PIPE_ASYNC), else NULL     */
-  /* LBM_PIPE_DIRECT only, optional: the indices (y * nseg + seg, ascending)
+  /* LBM_PIPE_DIRECT or LBM_PIPE_PREFETCH, optional: the indices (y * nseg + seg, ascending)
    * of every segment whose seg_flags entry is nonzero.  With it a step is two
    * launches, a lean kernel over the plain segments and a general one over
    * the listed segments; NULL keeps one general launch per step.          */
@@ -283,6 +288,12 @@ typedef struct LbmPlanBuffers {
    * the plain segments are launched and joined back after them, so the two
    * kernels overlap; 0 = both on the caller's stream, one after the other */
   int32_t special_stream;
+  /* LBM_PIPE_PREFETCH with a special list: the indices of every segment whose
+   * seg_flags entry is zero (ascending).  The plain segments then run on a
+   * persistent kernel whose warps load their next segment while colliding
+   * the current one.                                                       */
+  const int32_t* plain;
+  int32_t nplain;
 } LbmPlanBuffers;
 
 typedef struct LbmPlan LbmPlan;

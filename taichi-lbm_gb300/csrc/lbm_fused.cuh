@@ -51,6 +51,10 @@ struct FusedParams {
   // order, handled by k_fused_special; k_fused_bulk skips them
   const int32_t* special;
   int nspecial;
+  // prefetching two-pass step: the plain segments, same order
+  const int32_t* plain;
+  int nplain;
+  int tune;  // LBM_PIPE_ASYNC / LBM_PIPE_PREFETCH tuning index
   // 16-bit storage holds f_k - wsh[k], wsh[k] = w_k * rho_ref (the plan's
   // reference density); fp32 storage ignores it
   float wsh[9];

@@ -101,6 +101,34 @@ int launch_fused_persistent(const FusedParams& p, int pipeline, int tune, int32_
   }
 }
 
+template <int MODEL, bool PL, int ST, int V, int FORCE, int NW, int NS>
+int launch_pf_mp(const FusedParams& p, cudaStream_t s) {
+  static int blocks = 0;
+  auto kern = k_fused_bulk_pf<MODEL, PL, ST, V, FORCE, NW, NS>;
+  const int smem = NW * PfGeom<ST, V, NS>::WARP_BYTES;
+  int rc = persistent_blocks(kern, NW * 32, smem, &blocks);
+  if (rc) return rc;
+  kern<<<blocks, NW * 32, smem, s>>>(p);
+  return lbm_err::launch("fused step (plain segments, prefetching)");
+}
+
+template <int MODEL, bool PL, int ST, int V, int FORCE>
+int launch_pf_force(const FusedParams& p, cudaStream_t s) {
+  switch (p.tune) {  // (warps per block, stages per warp)
+    case 0: return launch_pf_mp<MODEL, PL, ST, V, FORCE, 8, 2>(p, s);
+    case 1: return launch_pf_mp<MODEL, PL, ST, V, FORCE, 8, 3>(p, s);
+    case 2: return launch_pf_mp<MODEL, PL, ST, V, FORCE, 4, 4>(p, s);
+    case 3: return launch_pf_mp<MODEL, PL, ST, V, FORCE, 16, 2>(p, s);
+    default: return lbm_err::set(LBM_ERR_ARG, "prefetch tuning %d (0..%d)", p.tune, LBM_PREFETCH_TUNINGS - 1);
+  }
+}
+
+template <int MODEL, bool PL, int ST, int V>
+int launch_pf_tuned(const FusedParams& p, cudaStream_t s) {
+  if (p.nplain == 0) return LBM_OK;
+  return p.has_force ? launch_pf_force<MODEL, PL, ST, V, 1>(p, s) : launch_pf_force<MODEL, PL, ST, V, 0>(p, s);
+}
+
 // The listed (flagged) segments on stream s2, then the plain segments, with
 // a compile-time force switch, on s.  s2 == s serialises the two; a caller
 // passing another stream has forked it from s and joins it back after.
@@ -111,8 +139,15 @@ int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s, cudaS
     int rc = lbm_err::launch("fused step (flagged segments)");
     if (rc) return rc;
   }
-  if (p.has_force) k_fused_bulk<MODEL, PL, ST, V, 1><<<blocks, 256, 0, s>>>(p);
-  else k_fused_bulk<MODEL, PL, ST, V, 0><<<blocks, 256, 0, s>>>(p);
+  if constexpr (V >= AV) {
+    if (p.plain) return launch_pf_tuned<MODEL, PL, ST, V>(p, s);  // prefetching persistent form
+  }
+  (void)blocks;
+  const int wpb = p.nseg < 8 ? p.nseg : 8;  // warps per block
+  const unsigned gy = p.ny < 65535 ? (unsigned)p.ny : 65535u;
+  const dim3 grid((unsigned)((p.nseg + wpb - 1) / wpb), gy, (unsigned)((p.ny + gy - 1) / gy));
+  if (p.has_force) k_fused_bulk<MODEL, PL, ST, V, 1><<<grid, 32 * wpb, 0, s>>>(p);
+  else k_fused_bulk<MODEL, PL, ST, V, 0><<<grid, 32 * wpb, 0, s>>>(p);
   return lbm_err::launch("fused step (plain segments)");
 }
 

@@ -26,12 +26,9 @@ __device__ __forceinline__ float raw_to_float<LBM_STORE_F16S>(__half v) { return
 template <>
 __device__ __forceinline__ float raw_to_float<LBM_STORE_BF16S>(__nv_bfloat16 v) { return __bfloat162float(v); }
 
-// V consecutive stored values -> floats (no shift)
+// V stored values -> floats (no shift)
 template <int ST, int V>
-__device__ __forceinline__ void load_raw(const typename Storage<ST>::T* p, float (&c)[V]) {
-  using T = typename Storage<ST>::T;
-  T raw[V];
-  load_vec<T, V>(p, raw);
+__device__ __forceinline__ void raw_to_floats(const typename Storage<ST>::T (&raw)[V], float (&c)[V]) {
   if constexpr (ST == LBM_STORE_F32) {
 #pragma unroll
     for (int i = 0; i < V; ++i) c[i] = raw[i];
@@ -54,6 +51,61 @@ __device__ __forceinline__ void load_raw(const typename Storage<ST>::T* p, float
       c[i + 1] = u.y;
     }
   }
+}
+
+// Read-only global loads as volatile asm: the compiler may neither drop nor
+// sink them below a later branch, so a warp's population loads are in
+// flight before it learns (from the segment flag loaded beside them)
+// whether it keeps the segment.
+__device__ __forceinline__ void ldg_early(const void* p, uint4& r) {
+  asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+}
+__device__ __forceinline__ void ldg_early(const void* p, uint2& r) {
+  asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+}
+__device__ __forceinline__ void ldg_early(const void* p, unsigned int& r) {
+  asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(r) : "l"(p));
+}
+__device__ __forceinline__ void ldg_early(const void* p, unsigned short& r) {
+  asm volatile("ld.global.nc.u16 %0, [%1];" : "=h"(r) : "l"(p));
+}
+__device__ __forceinline__ void ldg_early(const void* p, unsigned char& r) {
+  unsigned short t;
+  asm volatile("ld.global.nc.u8 %0, [%1];" : "=h"(t) : "l"(p));
+  r = (unsigned char)t;
+}
+
+// V consecutive elements (aligned), pieces of at most 16 B
+template <typename T, int V>
+__device__ __forceinline__ void load_vec_early(const T* p, T (&out)[V]) {
+  constexpr int B = sizeof(T) * V > 16 ? 16 : sizeof(T) * V;
+  constexpr int E = B / sizeof(T);
+  using R = typename Raw<B>::type;
+#pragma unroll
+  for (int c = 0; c < V / E; ++c) {
+    R r;
+    ldg_early(p + c * E, r);
+    memcpy(&out[c * E], &r, B);
+  }
+}
+template <typename T>
+__device__ __forceinline__ T load1_early(const T* p) {
+  typename Raw<sizeof(T)>::type r;
+  ldg_early(p, r);
+  T out;
+  memcpy(&out, &r, sizeof(T));
+  return out;
+}
+
+// V consecutive stored values -> floats (no shift)
+template <int ST, int V>
+__device__ __forceinline__ void load_raw(const typename Storage<ST>::T* p, float (&c)[V]) {
+  using T = typename Storage<ST>::T;
+  T raw[V];
+  load_vec_early<T, V>(p, raw);
+  raw_to_floats<ST, V>(raw, c);
 }
 
 // V floats -> V consecutive stored values (round to nearest, no shift)
@@ -100,13 +152,13 @@ __device__ __forceinline__ void gather_interior(const FusedParams& p, int y, int
       for (int i = 0; i < V; ++i) h[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0) left = raw_to_float<ST>(load1(row - 1));
+      if (lane == 0) left = raw_to_float<ST>(load1_early(row - 1));
       h[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31) right = raw_to_float<ST>(load1(row + V));
+      if (lane == 31) right = raw_to_float<ST>(load1_early(row + V));
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];
       h[V - 1][k] = right;
@@ -138,18 +190,18 @@ __device__ __forceinline__ void gather_edge(const FusedParams& p, int y, int x0,
       for (int i = 0; i < V; ++i) h[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0 && live) left = raw_to_float<ST>(load1(row + wrap(x0 - 1, p.nx)));
+      if (lane == 0 && live) left = raw_to_float<ST>(load1_early(row + wrap(x0 - 1, p.nx)));
       h[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31 && live) right = raw_to_float<ST>(load1(row + wrap(x0 + V, p.nx)));
+      if (lane == 31 && live) right = raw_to_float<ST>(load1_early(row + wrap(x0 + V, p.nx)));
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];
       h[V - 1][k] = right;
       if (live && ilast < V) {  // node nx-1 pulls from column 0
-        const float v0 = raw_to_float<ST>(load1(row));
+        const float v0 = raw_to_float<ST>(load1_early(row));
 #pragma unroll
         for (int i = 0; i < V; ++i)
           if (i == ilast) h[i][k] = v0;
@@ -162,18 +214,26 @@ __device__ __forceinline__ void gather_edge(const FusedParams& p, int y, int x0,
 // Shifted equilibria e_k = feq_k(rho, u) - wsh_k of all nine populations from
 // the pair decomposition feq_{k / opp k} = w_k rho (1 - 1.5 u.u + 4.5 (c_k.u)^2)
 // +- 3 w_k rho (c_k.u).
-__device__ __forceinline__ void shifted_feq(const FusedParams& p, float rho, float ux, float uy, float e[9]) {
+// SCALED: every e_k is multiplied by sc (BGK passes omega, so that the
+// relaxation h + omega (e - h) becomes one fma, (1 - omega) h + omega e).
+template <bool SCALED = false>
+__device__ __forceinline__ void shifted_feq(const FusedParams& p, float rho, float ux, float uy, float e[9],
+                                            float sc = 1.0f) {
   const float base = fmaf(-1.5f, fmaf(ux, ux, uy * uy), 1.0f);
-  const float r0 = rho * W(0), r1 = rho * W(1), r2 = rho * W(5);
+  const float rs = SCALED ? rho * sc : rho;
+  const float r0 = rs * W(0), r1 = rs * W(1), r2 = rs * W(5);
   const float a1 = 3.0f * r1, a2 = 3.0f * r2;
-  e[0] = fmaf(r0, base, -p.wsh[0]);
+  float w[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) w[k] = SCALED ? p.wsh[k] * sc : p.wsh[k];
+  e[0] = fmaf(r0, base, -w[0]);
   const float eu[4] = {ux, uy, ux + uy, uy - ux};  // c.u of k = 1, 2, 5, 6
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int k = q < 2 ? q + 1 : q + 3;
     const float r = q < 2 ? r1 : r2, a = q < 2 ? a1 : a2;
     const float t = fmaf(4.5f * eu[q], eu[q], base);
-    const float sym = fmaf(r, t, -p.wsh[k]);
+    const float sym = fmaf(r, t, -w[k]);
     const float anti = a * eu[q];
     e[k] = sym + anti;
     e[OPP(k)] = sym - anti;
@@ -206,13 +266,26 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
   const float jx = (h[1] - h[3]) + (h[5] - h[6]) + (h[8] - h[7]);
   const float jy = (h[2] - h[4]) + (h[5] + h[6]) - (h[7] + h[8]);
   const float Fx = FORCE == 1 ? p.gx : 0.0f, Fy = FORCE == 1 ? p.gy : 0.0f;
-  const float inv = 1.0f / rho;
+  const float inv = __fdividef(1.0f, rho);  // within 2 ulp; rho is O(1) here
   const float ux = (FORCE == 1 ? fmaf(0.5f, Fx, jx) : jx) * inv;
   const float uy = (FORCE == 1 ? fmaf(0.5f, Fy, jy) : jy) * inv;
-  float e[9];
-  shifted_feq(p, rho, ux, uy, e);
   float F[9];
   if (FORCE == 1) pair_force(Fx, Fy, ux, uy, F);
+  if (MODEL == LBM_BGK && !PL) {
+    // h' = (1 - omega) h + omega e (+ (1 - omega / 2) F)
+    const float om = p.omega, keep = 1.0f - om, cf = 1.0f - 0.5f * om;
+    float e[9];
+    shifted_feq<true>(p, rho, ux, uy, e, om);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      float v = fmaf(keep, h[k], e[k]);
+      if (FORCE == 1) v = fmaf(cf, F[k], v);
+      h[k] = v;
+    }
+    return state;
+  }
+  float e[9];
+  shifted_feq(p, rho, ux, uy, e);
 
   if (MODEL == LBM_MRT) {
     // m = M h; equilibrium moments less the moments of the shift (M wsh)
@@ -288,25 +361,11 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
   return state;
 }
 
-// Two-pass form of the direct step.  k_fused_bulk takes the plain segments
-// (seg_flags == 0), with the body force fixed at compile time, and leaves the
-// flagged segments to k_fused_special (lbm_fused.cuh), which walks the
-// compact list p.special of their indices (y * nseg + seg).  The two write
-// disjoint nodes and read only the source state, so they may run in either
-// order or concurrently within a step.
+// Moments, collision and stores of one lane's V nodes (x0.., row y) of a
+// plain segment, from the gathered stored values h.
 template <int MODEL, bool PL, int ST, int V, int FORCE>
-__global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
+__device__ __forceinline__ void lean_collide_store(const FusedParams& p, float (&h)[V][9], int y, int x0) {
   using T = typename Storage<ST>::T;
-  const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= (long long)p.ny * p.nseg) return;
-  if (p.seg_flags[warp]) return;  // uniform over the warp
-  const int y = (int)(warp / p.nseg);
-  const int seg = (int)(warp - (long long)y * p.nseg);
-  const int x0s = seg * 32 * V, x0 = x0s + lane * V;
-  float h[V][9];
-  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<ST, V>(p, y, x0, lane, h);
-  else gather_edge<ST, V>(p, y, x0, lane, h);
   const bool live = x0 < p.nx;
   const size_t rowoff = (size_t)y * p.pitch;
   float tau[V];
@@ -333,6 +392,207 @@ __global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
     for (int i = 0; i < V; ++i) c[i] = h[i][k];
     store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, c);
   }
+}
+
+// Two-pass form of the direct step.  k_fused_bulk takes the plain segments
+// (seg_flags == 0), with the body force fixed at compile time, and leaves the
+// flagged segments to k_fused_special (lbm_fused.cuh), which walks the
+// compact list p.special of their indices (y * nseg + seg).  The two write
+// disjoint nodes and read only the source state, so they may run in either
+// order or concurrently within a step.
+// Grid, in dispatch order: blockIdx.x * warps-per-block + warp = segment,
+// then row y = blockIdx.y + gridDim.y * blockIdx.z; resident blocks thus
+// cover a band of consecutive whole rows (DRAM page locality).
+template <int MODEL, bool PL, int ST, int V, int FORCE>
+__global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
+  const int lane = threadIdx.x & 31;
+  const int y = blockIdx.y + gridDim.y * blockIdx.z;
+  const int seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (seg >= p.nseg || y >= p.ny) return;
+  unsigned char flag;
+  ldg_early(p.seg_flags + (size_t)y * p.nseg + seg, flag);
+  const int x0s = seg * 32 * V, x0 = x0s + lane * V;
+  float h[V][9];
+  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<ST, V>(p, y, x0, lane, h);
+  else gather_edge<ST, V>(p, y, x0, lane, h);
+  if (flag) return;  // uniform over the warp: k_fused_special owns this segment
+  lean_collide_store<MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+}
+
+// ------------------------------------------------------------ prefetching form
+// k_fused_bulk_pf: persistent warps walk the compact list p.plain of plain
+// segments.  Each warp owns a ring of NS shared-memory stages; a stage holds
+// what one segment needs from the source: every lane's V elements of the
+// nine pulled rows, copied by that lane with cp.async (no registers held
+// while in flight), and the 4-byte words that contain the elements across
+// the segment's edges.  A warp keeps NS - 1 segments of copies in flight
+// while it collides the current one, then reads its own stage back (each
+// lane reads only what it copied, so no barrier is needed; cp.async.wait_group
+// is the hardware wait for the lane's own copies).
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr __host__ __device__ int edge_slot(int k) {  // the six links with cx = +-1 -> 0..5
+  return k == 1 ? 0 : k == 5 ? 1 : k == 8 ? 2 : k == 3 ? 3 : k == 6 ? 4 : 5;
+}
+
+template <int ST, int V, int NS>
+struct PfGeom {
+  using T = typename Storage<ST>::T;
+  static constexpr int POP_BYTES = 32 * V * (int)sizeof(T);   // one pulled row chunk of a warp
+  static constexpr int EDGE_OFF = 9 * POP_BYTES;               // [6][32] words
+  static constexpr int ITEM_OFF = EDGE_OFF + 6 * 32 * 4;       // [32] segment index, per lane
+  static constexpr int STAGE_BYTES = ITEM_OFF + 32 * 4;
+  static constexpr int WARP_BYTES = NS * STAGE_BYTES;
+  static_assert(POP_BYTES % 16 == 0 && STAGE_BYTES % 16 == 0, "stages must stay 16-byte aligned");
+};
+
+// element x of a row, as the 4-byte word that holds it (16-bit storage: the
+// even/odd pair; the word never passes the row's pitch, which is a multiple
+// of 32 elements)
+template <int ST>
+__device__ __forceinline__ const void* edge_word(const typename Storage<ST>::T* row, int x) {
+  return ST == LBM_STORE_F32 ? (const void*)(row + x) : (const void*)(row + (x & ~1));
+}
+template <int ST>
+__device__ __forceinline__ float edge_value(uint32_t w, int x) {
+  if constexpr (ST == LBM_STORE_F32) {
+    return __uint_as_float(w);
+  } else {
+    const unsigned short b = (unsigned short)((x & 1) ? (w >> 16) : (w & 0xffffu));
+    typename Storage<ST>::T t;
+    memcpy(&t, &b, 2);
+    return raw_to_float<ST>(t);
+  }
+}
+
+template <int ST, int V, int NS>
+__device__ __forceinline__ void pf_issue(const FusedParams& p, unsigned char* stage, int item, int lane) {
+  using T = typename Storage<ST>::T;
+  using G = PfGeom<ST, V, NS>;
+  if (item >= 0) {
+    const int y = item / p.nseg;
+    const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
+    const bool live = x0 < p.nx;
+    const int ilast = p.nx - 1 - x0;
+    const bool need_right = live && (lane == 31 || (ilast >= 0 && ilast < V));
+    const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
+    const int xr = x0 + V < p.nx ? x0 + V : 0;
+    const T* src = reinterpret_cast<const T*>(p.src);
+    uint32_t* edges = reinterpret_cast<uint32_t*>(stage + G::EDGE_OFF);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
+      if (live) cp_async<V * (int)sizeof(T)>(stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), row + x0);
+      if (CX(k) == 1 && lane == 0 && live) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xl));
+      if (CX(k) == -1 && need_right) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xr));
+    }
+    reinterpret_cast<int*>(stage + G::ITEM_OFF)[lane] = item;
+  }
+  cp_async_commit();
+}
+
+template <int MODEL, bool PL, int ST, int V, int FORCE, int NS>
+__device__ __forceinline__ void pf_consume(const FusedParams& p, const unsigned char* stage, int lane) {
+  using T = typename Storage<ST>::T;
+  using G = PfGeom<ST, V, NS>;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int item = reinterpret_cast<const int*>(stage + G::ITEM_OFF)[lane];
+  const int y = item / p.nseg;
+  const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
+  const bool live = x0 < p.nx;
+  const int ilast = p.nx - 1 - x0;
+  const bool has_last = ilast >= 0 && ilast < V;
+  const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
+  const int xr = x0 + V < p.nx ? x0 + V : 0;
+  const uint32_t* edges = reinterpret_cast<const uint32_t*>(stage + G::EDGE_OFF);
+  float h[V][9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    float c[V];
+    if (live) {
+      T raw[V];
+      memcpy(raw, stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), sizeof(raw));
+      raw_to_floats<ST, V>(raw, c);
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) c[i] = 0.0f;
+    }
+    if (CX(k) == 0) {
+#pragma unroll
+      for (int i = 0; i < V; ++i) h[i][k] = c[i];
+    } else if (CX(k) == 1) {
+      float left = __shfl_up_sync(FULL, c[V - 1], 1);
+      if (lane == 0 && live) left = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xl);
+      h[0][k] = left;
+#pragma unroll
+      for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
+    } else {
+      float right = __shfl_down_sync(FULL, c[0], 1);
+      float re = 0.0f;
+      if ((lane == 31 || has_last) && live) re = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xr);
+      if (lane == 31) right = re;
+#pragma unroll
+      for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];
+      h[V - 1][k] = right;
+      if (has_last) {  // node nx-1 pulls from column 0
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+          if (i == ilast) h[i][k] = re;
+      }
+    }
+  }
+  lean_collide_store<MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+}
+
+// blocks per SM the ring's shared memory allows (at most 2048 threads): the
+// register budget is set so that many blocks fit
+template <int ST, int V, int NW, int NS>
+constexpr int pf_min_blocks() {
+  constexpr int by_smem = (227 * 1024) / (NW * PfGeom<ST, V, NS>::WARP_BYTES);
+  constexpr int by_threads = 2048 / (NW * 32);
+  constexpr int b = by_smem < by_threads ? by_smem : by_threads;
+  return b < 1 ? 1 : b;
+}
+
+template <int MODEL, bool PL, int ST, int V, int FORCE, int NW, int NS>
+__global__ void __launch_bounds__(NW * 32, (pf_min_blocks<ST, V, NW, NS>())) k_fused_bulk_pf(const FusedParams p) {
+  using G = PfGeom<ST, V, NS>;
+  extern __shared__ __align__(16) unsigned char pf_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* ring = pf_smem + warp * G::WARP_BYTES;
+  const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
+  const int n = p.nplain;
+  if (gw >= n) return;
+#pragma unroll
+  for (int m = 0; m < NS - 1; ++m) {
+    const int pos = gw + m * GW;
+    pf_issue<ST, V, NS>(p, ring + m * G::STAGE_BYTES, pos < n ? p.plain[pos] : -1, lane);
+  }
+  int pos_next = gw + (NS - 1) * GW;
+  int item_next = pos_next < n ? p.plain[pos_next] : -1;  // read one iteration early
+  for (int m = 0;; ++m) {
+    if (gw + m * GW >= n) break;
+    const int pos_after = pos_next + GW;
+    const int item_after = pos_after < n ? p.plain[pos_after] : -1;
+    pf_issue<ST, V, NS>(p, ring + ((m + NS - 1) % NS) * G::STAGE_BYTES, item_next, lane);
+    cp_async_wait<NS - 1>();  // this lane's copies of segment m have landed
+    pf_consume<MODEL, PL, ST, V, FORCE, NS>(p, ring + (m % NS) * G::STAGE_BYTES, lane);
+    pos_next = pos_after;
+    item_next = item_after;
+  }
+  cp_async_wait<0>();
 }
 
 }  // namespace lbm

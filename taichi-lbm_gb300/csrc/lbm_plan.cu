@@ -40,8 +40,13 @@ FusedParams params_for(LbmPlan* pl) {
   p.code = pl->b.code;
   p.seg_flags = pl->b.seg_flags;
   p.tau = pl->b.tau;
-  p.special = pl->d.pipeline == LBM_PIPE_DIRECT && !pl->d.sc ? pl->b.special : nullptr;
-  p.nspecial = p.special ? pl->b.nspecial : 0;
+  // two-pass forms: direct (special list), prefetch (special and plain lists)
+  const bool two = !pl->d.sc && pl->b.special &&
+                   (pl->d.pipeline == LBM_PIPE_DIRECT || (pl->d.pipeline == LBM_PIPE_PREFETCH && pl->b.plain));
+  p.special = two ? pl->b.special : nullptr;
+  p.nspecial = two ? pl->b.nspecial : 0;
+  p.plain = two && pl->d.pipeline == LBM_PIPE_PREFETCH ? pl->b.plain : nullptr;
+  p.nplain = p.plain ? pl->b.nplain : 0;
   return p;
 }
 
@@ -54,7 +59,7 @@ int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, cudaStre
       default: return lbm::launch_fused_sc<LBM_STORE_BF16S>(p, s);
     }
   }
-  if (pipeline == LBM_PIPE_ASYNC || pipeline == LBM_PIPE_PREFETCH) {
+  if (pipeline == LBM_PIPE_ASYNC || (pipeline == LBM_PIPE_PREFETCH && !p.plain)) {
     switch (st) {
       case LBM_STORE_F32: return lbm::launch_fused_persistent<LBM_STORE_F32>(p, pipeline, tune, status, s);
       case LBM_STORE_F16S: return lbm::launch_fused_persistent<LBM_STORE_F16S>(p, pipeline, tune, status, s);
@@ -143,10 +148,13 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   if (!vok) return lbm_err::set(LBM_ERR_UNSUPPORTED, "nodes_per_thread %d for storage %d", V, d->storage);
   if (d->pipeline < LBM_PIPE_DIRECT || d->pipeline > LBM_PIPE_PREFETCH)
     return lbm_err::set(LBM_ERR_ARG, "pipeline %d", d->pipeline);
-  if (d->pipeline != LBM_PIPE_DIRECT && V != lbm::AV)
-    return lbm_err::set(LBM_ERR_UNSUPPORTED, "persistent pipelines run %d nodes per thread", lbm::AV);
+  if (d->pipeline != LBM_PIPE_DIRECT && V != lbm::AV && !(d->pipeline == LBM_PIPE_PREFETCH && V == 8))
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "persistent pipelines run %d nodes per thread (prefetch: also 8 "
+                        "with 16-bit storage)", lbm::AV);
   if (d->pipeline == LBM_PIPE_ASYNC && (d->tune < 0 || d->tune >= LBM_ASYNC_TUNINGS))
     return lbm_err::set(LBM_ERR_ARG, "async tuning %d", d->tune);
+  if (d->pipeline == LBM_PIPE_PREFETCH && (d->tune < 0 || d->tune >= LBM_PREFETCH_TUNINGS))
+    return lbm_err::set(LBM_ERR_ARG, "prefetch tuning %d", d->tune);
   if (d->sc) {
     if (d->pipeline != LBM_PIPE_DIRECT || V != lbm::AV)
       return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans run the direct pipeline, %d nodes per thread",
@@ -200,6 +208,7 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   p.g_coh = d->g_coh;
   p.sc_T = d->sc_T;
   p.eos = d->eos;
+  p.tune = d->tune;
   if (!(d->rho_ref >= 0.0f && d->rho_ref < 1e30f))
     return lbm_err::set(LBM_ERR_ARG, "rho_ref %g must be finite and >= 0", (double)d->rho_ref);
   const float rho_ref = d->rho_ref != 0.0f ? d->rho_ref : 1.0f;
@@ -233,6 +242,14 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
       (int64_t)b->nspecial > (int64_t)pl->d.ny * pl->base.nseg)
     return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d special segments for a %d x %d segment grid", b->nspecial,
                         pl->d.ny, pl->base.nseg);
+  if (b->nplain < 0 || (b->nplain > 0 && !b->plain) ||
+      (int64_t)b->nplain + b->nspecial > (int64_t)pl->d.ny * pl->base.nseg)
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d plain + %d special segments for a %d x %d segment grid",
+                        b->nplain, b->nspecial, pl->d.ny, pl->base.nseg);
+  if (pl->d.pipeline == LBM_PIPE_PREFETCH && pl->d.nodes_per_thread != lbm::AV && !pl->d.sc &&
+      !(b->special && b->plain))
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "plan_bind: the prefetch pipeline at %d nodes per thread needs the "
+                        "special and plain segment lists", pl->d.nodes_per_thread);
   pl->b = *b;
   pl->bound = true;
   pl->parity = 0;

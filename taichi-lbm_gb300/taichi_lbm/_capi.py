@@ -76,7 +76,8 @@ ASYNC_TUNINGS = 4
 class LbmPlanBuffers(ctypes.Structure):
     _fields_ = [(n, _vp) for n in ("fa", "fb", "mom_a", "mom_b", "code", "seg_flags", "bc_vel",
                                    "tau", "status", "special")] + [("nspecial", ctypes.c_int32),
-                                                           ("special_stream", ctypes.c_int32)]
+                                                           ("special_stream", ctypes.c_int32),
+                                                           ("plain", _vp), ("nplain", ctypes.c_int32)]
 
 
 class LbmError(RuntimeError):

@@ -73,7 +73,8 @@ class FusedSolver:
         self.pipeline = PIPELINE[pipeline] if isinstance(pipeline, str) else int(pipeline)
         self.V = int(nodes_per_thread or DEFAULT_V[self.storage])
         self.tune = int(tune)
-        if self.pipeline != A.PIPE_DIRECT:
+        if self.pipeline != A.PIPE_DIRECT and not (self.pipeline == A.PIPE_PREFETCH and self.V == 8
+                                                   and self.storage != A.STORE_F32 and two_pass):
             self.V = 4
         self.status = torch.zeros(1, dtype=torch.int32, device=lb_field.device)
         if local_relaxation is None:
@@ -195,9 +196,13 @@ class FusedSolver:
         d.rho_ref = self._rho_ref()
         self.desc = d
         # flagged segments, listed for the two-pass direct step
-        flagged = np.flatnonzero(np.asarray(cp.seg_flags).ravel()).astype(np.int32)
+        flags = np.asarray(cp.seg_flags).ravel()
+        flagged = np.flatnonzero(flags).astype(np.int32)
+        plain = np.flatnonzero(flags == 0).astype(np.int32)
         self.special = torch.as_tensor(flagged if flagged.size else np.zeros(1, np.int32), device=dev)
         self.nspecial = int(flagged.size)
+        self.plain = torch.as_tensor(plain if plain.size else np.zeros(1, np.int32), device=dev)
+        self.nplain = int(plain.size)
         self.mom = [torch.zeros((3, ny, P), dtype=torch.float32, device=dev) for _ in range(2)]
         if self.storage == A.STORE_F32:
             self.fbuf = None
@@ -230,9 +235,11 @@ class FusedSolver:
         b.bc_vel = None if self.bc_vel is None else self.bc_vel.data_ptr()
         b.tau = self.tau_state.data_ptr() if self.powerlaw else None
         b.status = self.status.data_ptr()
-        if self.two_pass and self.pipeline == A.PIPE_DIRECT:
+        if self.two_pass and self.pipeline in (A.PIPE_DIRECT, A.PIPE_PREFETCH):
             b.special, b.nspecial = self.special.data_ptr(), self.nspecial
             b.special_stream = 1 if self.overlap else 0
+            if self.pipeline == A.PIPE_PREFETCH:
+                b.plain, b.nplain = self.plain.data_ptr(), self.nplain
         A.call("lbm_plan_bind", self._plan, ctypes.byref(b))
 
     def _moments(self):
@@ -272,7 +279,8 @@ class FusedSolver:
     def launches_per_step(self):
         """Kernel launches of one lbm_plan_run step: two for the two-pass
         direct step (plain segments, then the listed ones), else one."""
-        if self.sc is None and self.pipeline == A.PIPE_DIRECT and self.two_pass and self.nspecial:
+        if (self.sc is None and self.pipeline in (A.PIPE_DIRECT, A.PIPE_PREFETCH) and self.two_pass
+                and self.nspecial and (self.nplain or self.pipeline == A.PIPE_DIRECT)):
             return 2
         return 1
 

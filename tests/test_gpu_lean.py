@@ -66,13 +66,14 @@ def check_storage(got, ref64, storage):
     assert rel_err(got["vel"], ref64["vel"]) < 10 * tol
 
 
+@pytest.mark.parametrize("pipeline", ["direct", "prefetch"])
 @pytest.mark.parametrize("gravity", [False, True])
 @pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
-def test_lean_periodic_box(tl, model, storage, gravity):
+def test_lean_periodic_box(tl, model, storage, gravity, pipeline):
     lb, me, coll, be = periodic_box(tl, model, tl.NewtonianFluid(0.05), gravity)
     meta, arrays = describe(lb, coll, be, 120)
-    solver = tl.FusedSolver(lb, me, coll, be, storage=storage)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, pipeline=pipeline)
     assert solver.nspecial == 0  # every segment takes the lean kernel
     solver.step(120)
     got = fields_of(lb)
@@ -82,12 +83,13 @@ def test_lean_periodic_box(tl, model, storage, gravity):
         check_storage(got, fp64_solution(meta, arrays), storage)
 
 
+@pytest.mark.parametrize("pipeline", ["direct", "prefetch"])
 @pytest.mark.parametrize("storage", ["fp32", "fp16s"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
-def test_lean_periodic_box_power_law(tl, model, storage):
+def test_lean_periodic_box_power_law(tl, model, storage, pipeline):
     lb, me, coll, be = periodic_box(tl, model, tl.PowerLawFluid(0.02, 0.7), True)
     meta, arrays = describe(lb, coll, be, 100, step_kind="powerlaw")
-    tl.FusedSolver(lb, me, coll, be, storage=storage).step(100)
+    tl.FusedSolver(lb, me, coll, be, storage=storage, pipeline=pipeline).step(100)
     got = fields_of(lb)
     if storage == "fp32":
         check_parity(got, O.replay(meta, arrays), fp64_solution(meta, arrays), ("f", "rho", "vel"), TOL_PL)
@@ -119,3 +121,21 @@ def test_two_pass_forms_agree(tl, model, storage):
         check_parity(out[2], O.replay(meta, arrays), fp64_solution(meta, arrays), ("f", "rho", "vel"), TOL)
     else:
         check_storage(out[2], fp64_solution(meta, arrays), storage)
+
+
+@pytest.mark.parametrize("tune", [0, 1, 2, 3])
+@pytest.mark.parametrize("shape", [(520, 64), (389, 40)])
+def test_prefetch_tunings_match_direct(tl, tune, shape):
+    """Every shared-memory ring shape of the prefetching kernel gives the
+    direct pipeline's result to the bit (same arithmetic, other loads); 389
+    columns put node nx-1 inside a lane of a partial segment."""
+    nx, ny = shape
+    out = []
+    for pipeline, t in (("direct", 0), ("prefetch", tune)):
+        lb, me, coll, be = cylinder_channel(tl, nx, ny, ny / 10, nx / 5, ny / 2 - 0.5, 0.56, 0.05, model="trt")
+        solver = tl.FusedSolver(lb, me, coll, be, storage="fp16s", pipeline=pipeline, tune=t)
+        assert solver.launches_per_step == 2
+        solver.step(60)
+        out.append(fields_of(lb))
+    for k in ("f", "f2", "rho", "vel"):
+        assert rel_err(out[1][k], out[0][k]) == 0.0, k
