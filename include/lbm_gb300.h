@@ -353,6 +353,40 @@ int lbm_plan_reduce_moments(LbmPlan* plan, double* partials, double* out, void* 
 #define LBM_NOALLOC_MAX_NODES (2048LL * LBM_NOALLOC_CHUNK)
 int lbm_plan_reduce_moments_noalloc(LbmPlan* plan, double* out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batches: many independent lattices advanced together.  No counterpart in
+ * the reference (taichi-lbm steps one LBField per Python loop); the serving
+ * and batching layers of this library are built on it.
+ *
+ * A batch holds bound plans.  lbm_batch_run advances every member nsteps
+ * steps: per step, one persistent launch per group of members that share a
+ * kernel (plain segments, flagged segments or Shan-Chen tiles x collision
+ * model x power law x storage x nodes per thread x body force), walking a
+ * packed table of (member, tile) entries, then the members' drag/lift
+ * monitors.  Results equal lbm_plan_run on each member alone.  Member plans'
+ * parities advance with the batch; a plan must not be run on its own while
+ * it is a member.  The batch runs on its own stream, ordered after the
+ * caller's stream by an event and joined back to it the same way.  With
+ * graphs on, two steps are captured once per membership and replayed.
+ * Adding, removing or re-monitoring a member rebuilds the tables at the next
+ * run; removal waits for the batch's launched work.                        */
+typedef struct LbmBatch LbmBatch;
+int lbm_batch_create(LbmBatch** out);
+int lbm_batch_add(LbmBatch* batch, LbmPlan* plan, int32_t* slot);
+int lbm_batch_remove(LbmBatch* batch, int32_t slot);
+/* After every step, append the member's momentum-exchange force (Fx, Fy) on
+ * its solid links (site, k pairs, as lbm_plan_momentum_exchange) to
+ * series[2 * (*count)] while *count < capacity, and increment *count
+ * (device int32, set by the caller). */
+int lbm_batch_monitor(LbmBatch* batch, int32_t slot, const int32_t* links, int64_t nlinks, double* series,
+                      int32_t* count, int32_t capacity);
+int lbm_batch_set_graph(LbmBatch* batch, int32_t enable);
+int lbm_batch_run(LbmBatch* batch, int32_t nsteps, void* stream);
+/* members; tiles and groups of the current tables (-1 before the first run
+ * after a change) */
+int lbm_batch_info(const LbmBatch* batch, int32_t* members, int64_t* tiles, int32_t* groups);
+int lbm_batch_destroy(LbmBatch* batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,10 @@ OUT_DIR = os.path.join(HERE, "taichi_lbm", "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liblbm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--use_fast_math=false"]
+# -fmad=false: no implicit fma contraction, so a node computes bit for bit
+# alike in every kernel that shares the source (fused multiply-adds are
+# written out as fmaf where the hot paths want them)
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--use_fast_math=false", "-fmad=false"]
 
 
 def _nvcc():

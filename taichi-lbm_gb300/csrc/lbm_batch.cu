@@ -1,0 +1,417 @@
+// Batch of independent lattices advanced together (C ABI: lbm_batch_*).
+//
+// A batch holds bound plans ("members").  On the first run after a change of
+// membership it groups the members by kernel kind (Shan-Chen tile, plain
+// segment, flagged segment) x collision model x power law x storage x nodes
+// per lane x body force, writes one device record per member (its parameters
+// for both ping-pong parities) and one packed tile table, and from then on a
+// step is one persistent launch per group, followed by the drag/lift monitors.
+// The batch runs on its own stream, forked from and joined back to the
+// caller's stream; with graphs enabled it captures two steps (parities 0 and
+// 1) once per membership and replays them.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <tuple>
+#include <vector>
+
+#include "lbm_batch.cuh"
+#include "lbm_plan_internal.h"
+
+LBM_BATCH_EXTERN(LBM_STORE_F32)
+LBM_BATCH_EXTERN(LBM_STORE_F16S)
+LBM_BATCH_EXTERN(LBM_STORE_BF16S)
+
+using lbm::BatchGroup;
+using lbm::BatchLattice;
+using lbm::BatchMonitor;
+using lbm::BatchTile;
+
+struct BatchMember {
+  LbmPlan* plan = nullptr;
+  bool monitored = false;
+  const int32_t* links = nullptr;
+  int64_t nlinks = 0;
+  double* series = nullptr;
+  int32_t* count = nullptr;
+  int32_t capacity = 0;
+};
+
+struct LbmBatch {
+  std::vector<BatchMember> slots;  // plan == nullptr: free slot
+  bool dirty = true;
+  long long step = 0;  // steps run; parity = step & 1
+  int dev = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  // device tables
+  BatchLattice* d_lats = nullptr;
+  size_t lats_cap = 0;
+  BatchTile* d_tiles = nullptr;
+  size_t tiles_cap = 0;
+  BatchMonitor* d_mons = nullptr;
+  size_t mons_cap = 0;
+  std::vector<BatchGroup> groups;
+  int mon_off[3] = {0, 0, 0}, mon_cnt[3] = {0, 0, 0};  // monitors per storage
+  long long ntiles = 0;
+  int nlats = 0;
+  // graphs
+  bool use_graph = false;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_ok = false;
+};
+
+namespace {
+
+int launch_group(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
+  switch (g.storage) {
+    case LBM_STORE_F32: return lbm::launch_batch_group<LBM_STORE_F32>(g, lats, tiles, sp, s);
+    case LBM_STORE_F16S: return lbm::launch_batch_group<LBM_STORE_F16S>(g, lats, tiles, sp, s);
+    default: return lbm::launch_batch_group<LBM_STORE_BF16S>(g, lats, tiles, sp, s);
+  }
+}
+
+int launch_monitors(LbmBatch* b, int sp, cudaStream_t s) {
+  for (int st = 0; st < 3; ++st) {
+    if (!b->mon_cnt[st]) continue;
+    const BatchMonitor* m = b->d_mons + b->mon_off[st];
+    int rc = st == LBM_STORE_F32    ? lbm::launch_batch_monitors<LBM_STORE_F32>(b->d_lats, m, b->mon_cnt[st], sp, s)
+             : st == LBM_STORE_F16S ? lbm::launch_batch_monitors<LBM_STORE_F16S>(b->d_lats, m, b->mon_cnt[st], sp, s)
+                                    : lbm::launch_batch_monitors<LBM_STORE_BF16S>(b->d_lats, m, b->mon_cnt[st], sp, s);
+    if (rc) return rc;
+  }
+  return LBM_OK;
+}
+
+// one batched step at parity sp on stream s
+int batch_step(LbmBatch* b, int sp, cudaStream_t s) {
+  for (BatchGroup& g : b->groups) {
+    int rc = launch_group(g, b->d_lats, b->d_tiles, sp, s);
+    if (rc) return rc;
+  }
+  return launch_monitors(b, sp, s);
+}
+
+void drop_graph(LbmBatch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->graph_ok = false;
+}
+
+template <typename T>
+int ensure_capacity(T** ptr, size_t* cap, size_t n, const char* what) {
+  if (n <= *cap && *ptr) return LBM_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  const size_t want = std::max<size_t>(n, 1);
+  int rc = lbm_err::cuda(cudaMalloc(reinterpret_cast<void**>(ptr), want * sizeof(T)), what);
+  if (rc) return rc;
+  *cap = want;
+  return LBM_OK;
+}
+
+int ensure_stream(LbmBatch* b) {
+  int dev = 0;
+  int rc = lbm_err::cuda(cudaGetDevice(&dev), "batch: device");
+  if (rc) return rc;
+  if (b->stream && b->dev == dev) return LBM_OK;
+  if (b->stream) return lbm_err::set(LBM_ERR_STATE, "batch: created on device %d, used on device %d", b->dev, dev);
+  rc = lbm_err::cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "batch: stream");
+  if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch: event");
+  if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "batch: event");
+  if (rc) return rc;
+  b->dev = dev;
+  return LBM_OK;
+}
+
+struct GroupKey {
+  int kind, model, powerlaw, storage, V, force;
+  bool operator<(const GroupKey& o) const {
+    return std::tie(kind, storage, model, powerlaw, V, force) <
+           std::tie(o.kind, o.storage, o.model, o.powerlaw, o.V, o.force);
+  }
+  bool operator==(const GroupKey& o) const {
+    return kind == o.kind && model == o.model && powerlaw == o.powerlaw && storage == o.storage && V == o.V &&
+           force == o.force;
+  }
+};
+
+// rebuild the device records and tile tables from the current members
+int rebuild(LbmBatch* b) {
+  // the previous tables may still be read by launched work
+  int rc = lbm_err::cuda(cudaStreamSynchronize(b->stream), "batch: synchronize before rebuild");
+  if (rc) return rc;
+  drop_graph(b);
+  const int sp = (int)(b->step & 1);
+  std::vector<BatchLattice> lats;
+  std::map<GroupKey, std::vector<BatchTile>> by_key;  // references stay valid as keys are added
+  auto bucket = [&](const GroupKey& k) -> std::vector<BatchTile>& { return by_key[k]; };
+  std::vector<BatchMonitor> mons[3];
+  std::vector<uint8_t> flags;
+  for (BatchMember& m : b->slots) {
+    if (!m.plan) continue;
+    LbmPlan* pl = m.plan;
+    const int lat = (int)lats.size();
+    BatchLattice rec;
+    std::memset(&rec, 0, sizeof(rec));
+    const int saved = pl->parity;
+    for (int v = 0; v < 2; ++v) {
+      pl->parity = v;
+      rec.full[v] = lbm_plan_params(pl);
+      rec.full[v].special = nullptr;  // the batch supplies its own tiles
+      rec.full[v].plain = nullptr;
+      rec.lean[v] = lbm::lean_of(rec.full[v]);
+    }
+    pl->parity = saved;
+    rec.flip = saved ^ sp;
+    lats.push_back(rec);
+    const lbm::FusedParams& p = rec.full[0];
+    const int pw = pl->d.fluid_model == LBM_POWERLAW ? 1 : 0;
+    if (pl->d.sc) {
+      auto& t = bucket({lbm::BATCH_SC, pl->d.model, 0, pl->d.storage, pl->d.nodes_per_thread, 1});
+      const int tiles_y = p.ny / lbm::SC_ROWS;
+      for (int ty = 0; ty < tiles_y; ++ty)
+        for (int seg = 0; seg < p.nseg; ++seg) t.push_back({lat, ty + tiles_y * seg});
+    } else {
+      flags.resize((size_t)p.ny * p.nseg);
+      rc = lbm_err::cuda(cudaMemcpy(flags.data(), pl->b.seg_flags, flags.size(), cudaMemcpyDeviceToHost),
+                         "batch: segment flags");
+      if (rc) return rc;
+      auto& tl = bucket({lbm::BATCH_LEAN, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, p.has_force});
+      auto& ts = bucket({lbm::BATCH_SPECIAL, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, 0});
+      for (int item = 0; item < (int)flags.size(); ++item) (flags[item] ? ts : tl).push_back({lat, item});
+    }
+    if (m.monitored) {
+      BatchMonitor bm;
+      bm.lat = lat;
+      bm.nlinks = m.nlinks;
+      bm.links = m.links;
+      bm.series = m.series;
+      bm.count = m.count;
+      bm.capacity = m.capacity;
+      mons[pl->d.storage].push_back(bm);
+    }
+  }
+  // plain groups first (the bulk of the work), then Shan-Chen, then flagged:
+  // the key order starts with the kind
+  std::vector<std::pair<GroupKey, std::vector<BatchTile>>> buckets(by_key.begin(), by_key.end());
+  std::vector<BatchTile> tiles;
+  b->groups.clear();
+  for (auto& e : buckets) {
+    if (e.second.empty()) continue;
+    BatchGroup g;
+    g.kind = e.first.kind;
+    g.model = e.first.model;
+    g.powerlaw = e.first.powerlaw;
+    g.storage = e.first.storage;
+    g.V = e.first.V;
+    g.force = e.first.force;
+    g.offset = (int)tiles.size();
+    g.count = (int)e.second.size();
+    g.blocks = 0;
+    tiles.insert(tiles.end(), e.second.begin(), e.second.end());
+    b->groups.push_back(g);
+  }
+  if (tiles.size() > (size_t)INT32_MAX) return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch: too many tiles");
+  std::vector<BatchMonitor> allm;
+  for (int st = 0; st < 3; ++st) {
+    b->mon_off[st] = (int)allm.size();
+    b->mon_cnt[st] = (int)mons[st].size();
+    allm.insert(allm.end(), mons[st].begin(), mons[st].end());
+  }
+  rc = ensure_capacity(&b->d_lats, &b->lats_cap, lats.size(), "batch: lattice records");
+  if (!rc) rc = ensure_capacity(&b->d_tiles, &b->tiles_cap, tiles.size(), "batch: tile table");
+  if (!rc) rc = ensure_capacity(&b->d_mons, &b->mons_cap, allm.size(), "batch: monitors");
+  if (rc) return rc;
+  if (!lats.empty())
+    rc = lbm_err::cuda(cudaMemcpy(b->d_lats, lats.data(), lats.size() * sizeof(BatchLattice), cudaMemcpyHostToDevice),
+                       "batch: upload records");
+  if (!rc && !tiles.empty())
+    rc = lbm_err::cuda(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice),
+                       "batch: upload tiles");
+  if (!rc && !allm.empty())
+    rc = lbm_err::cuda(cudaMemcpy(b->d_mons, allm.data(), allm.size() * sizeof(BatchMonitor), cudaMemcpyHostToDevice),
+                       "batch: upload monitors");
+  if (rc) return rc;
+  b->ntiles = (long long)tiles.size();
+  b->nlats = (int)lats.size();
+  b->dirty = false;
+  return LBM_OK;
+}
+
+int capture(LbmBatch* b) {
+  // two steps, parities 0 and 1, on the batch stream
+  cudaGraph_t graph = nullptr;
+  int rc = lbm_err::cuda(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch: begin capture");
+  if (rc) return rc;
+  int rs = batch_step(b, 0, b->stream);
+  if (!rs) rs = batch_step(b, 1, b->stream);
+  rc = lbm_err::cuda(cudaStreamEndCapture(b->stream, &graph), "batch: end capture");
+  if (rs) rc = rs;
+  if (!rc) rc = lbm_err::cuda(cudaGraphInstantiate(&b->exec, graph, 0), "batch: instantiate graph");
+  if (graph) cudaGraphDestroy(graph);
+  if (rc) {
+    drop_graph(b);
+    return rc;
+  }
+  b->graph_ok = true;
+  return LBM_OK;
+}
+
+// advance the parity bookkeeping of the batch and of every member plan
+void advance(LbmBatch* b, int n) {
+  b->step += n;
+  if (n & 1)
+    for (BatchMember& m : b->slots)
+      if (m.plan) m.plan->parity ^= 1;
+}
+
+int run_on_stream(LbmBatch* b, int32_t nsteps) {
+  cudaStream_t s = b->stream;
+  int done = 0;
+  if (b->use_graph && nsteps >= 3 && b->nlats > 0) {
+    if (!b->graph_ok) {  // a direct step sizes every persistent grid before the capture
+      int rc = batch_step(b, (int)(b->step & 1), s);
+      if (rc) return rc;
+      advance(b, 1);
+      ++done;
+    }
+    if (b->step & 1) {  // the graph starts at parity 0
+      int rc = batch_step(b, 1, s);
+      if (rc) return rc;
+      advance(b, 1);
+      ++done;
+    }
+    if (!b->graph_ok && nsteps - done >= 2) {
+      int rc = capture(b);
+      if (rc) return rc;
+    }
+    while (b->graph_ok && nsteps - done >= 2) {
+      int rc = lbm_err::cuda(cudaGraphLaunch(b->exec, s), "batch: graph launch");
+      if (rc) return rc;
+      advance(b, 2);
+      done += 2;
+    }
+  }
+  while (done < nsteps) {
+    int rc = batch_step(b, (int)(b->step & 1), s);
+    if (rc) return rc;
+    advance(b, 1);
+    ++done;
+  }
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(LbmBatch** out) {
+  if (!out) return lbm_err::set(LBM_ERR_ARG, "batch_create: NULL argument");
+  *out = new (std::nothrow) LbmBatch();
+  return *out ? LBM_OK : lbm_err::set(LBM_ERR_ARG, "batch_create: out of host memory");
+}
+
+int lbm_batch_add(LbmBatch* b, LbmPlan* plan, int32_t* slot) {
+  if (!b || !plan || !slot) return lbm_err::set(LBM_ERR_ARG, "batch_add: NULL argument");
+  if (!plan->bound) return lbm_err::set(LBM_ERR_STATE, "batch_add: plan not bound");
+  const LbmPlanDesc& d = plan->d;
+  const int V = d.nodes_per_thread;
+  if (d.sc && V != lbm::AV)
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch_add: Shan-Chen members run %d nodes per lane", lbm::AV);
+  if (d.storage == LBM_STORE_F32 ? (V != 2 && V != 4) : (V != 4 && V != 8))
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch_add: nodes_per_thread %d for storage %d", V, d.storage);
+  for (const BatchMember& m : b->slots)
+    if (m.plan == plan) return lbm_err::set(LBM_ERR_ARG, "batch_add: plan is already a member");
+  size_t i = 0;
+  while (i < b->slots.size() && b->slots[i].plan) ++i;
+  if (i == b->slots.size()) b->slots.emplace_back();
+  b->slots[i] = BatchMember();
+  b->slots[i].plan = plan;
+  b->dirty = true;
+  *slot = (int32_t)i;
+  return LBM_OK;
+}
+
+int lbm_batch_monitor(LbmBatch* b, int32_t slot, const int32_t* links, int64_t nlinks, double* series,
+                      int32_t* count, int32_t capacity) {
+  if (!b || slot < 0 || slot >= (int32_t)b->slots.size() || !b->slots[slot].plan)
+    return lbm_err::set(LBM_ERR_ARG, "batch_monitor: no member in slot %d", slot);
+  if (nlinks < 0 || (nlinks > 0 && !links) || !series || !count || capacity < 0)
+    return lbm_err::set(LBM_ERR_ARG, "batch_monitor: bad arguments");
+  BatchMember& m = b->slots[slot];
+  m.monitored = true;
+  m.links = links;
+  m.nlinks = nlinks;
+  m.series = series;
+  m.count = count;
+  m.capacity = capacity;
+  b->dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_remove(LbmBatch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int32_t)b->slots.size() || !b->slots[slot].plan)
+    return lbm_err::set(LBM_ERR_ARG, "batch_remove: no member in slot %d", slot);
+  // launched work may still read the member's buffers through the tables
+  if (b->stream) {
+    int rc = lbm_err::cuda(cudaStreamSynchronize(b->stream), "batch_remove: synchronize");
+    if (rc) return rc;
+  }
+  b->slots[slot] = BatchMember();
+  b->dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_set_graph(LbmBatch* b, int32_t enable) {
+  if (!b) return lbm_err::set(LBM_ERR_ARG, "batch_set_graph: NULL batch");
+  b->use_graph = enable != 0;
+  if (!b->use_graph) drop_graph(b);
+  return LBM_OK;
+}
+
+int lbm_batch_run(LbmBatch* b, int32_t nsteps, void* stream) {
+  if (!b) return lbm_err::set(LBM_ERR_ARG, "batch_run: NULL batch");
+  if (nsteps < 0) return lbm_err::set(LBM_ERR_ARG, "batch_run: nsteps %d", nsteps);
+  if (nsteps == 0) return LBM_OK;
+  int rc = ensure_stream(b);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = lbm_err::cuda(cudaEventRecord(b->fork, s), "batch_run: fork");
+  if (!rc) rc = lbm_err::cuda(cudaStreamWaitEvent(b->stream, b->fork, 0), "batch_run: fork");
+  if (rc) return rc;
+  if (b->dirty) rc = rebuild(b);
+  if (!rc) rc = run_on_stream(b, nsteps);
+  // join even after a failure, so the caller's stream never runs ahead
+  int rj = lbm_err::cuda(cudaEventRecord(b->join, b->stream), "batch_run: join");
+  if (!rj) rj = lbm_err::cuda(cudaStreamWaitEvent(s, b->join, 0), "batch_run: join");
+  return rc ? rc : rj;
+}
+
+int lbm_batch_info(const LbmBatch* b, int32_t* members, int64_t* tiles, int32_t* groups) {
+  if (!b) return lbm_err::set(LBM_ERR_ARG, "batch_info: NULL batch");
+  int n = 0;
+  for (const BatchMember& m : b->slots) n += m.plan ? 1 : 0;
+  if (members) *members = n;
+  if (tiles) *tiles = b->dirty ? -1 : b->ntiles;
+  if (groups) *groups = b->dirty ? -1 : (int32_t)b->groups.size();
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(LbmBatch* b) {
+  if (!b) return LBM_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  if (b->d_lats) cudaFree(b->d_lats);
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->d_mons) cudaFree(b->d_mons);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return LBM_OK;
+}
+
+}  // extern "C"

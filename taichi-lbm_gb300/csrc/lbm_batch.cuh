@@ -1,0 +1,271 @@
+// Batched kernels: many independent lattices advance one time step in one
+// launch per kernel kind, over a packed tile table.
+//
+// Every lattice has a device record with two views of its parameters (the
+// populations and saved moments read from / written to, for the two
+// ping-pong parities).  A tile is (lattice, item): for the plain and flagged
+// kinds an item is one row segment (y * nseg + seg), for Shan-Chen one
+// SC_ROWS x 32V block tile.  The kernels are persistent: a grid sized to the
+// GPU walks the table, a warp (or, for Shan-Chen, a block) per tile, and
+// copies a lattice's parameters into shared memory when its tile belongs to
+// another lattice than the previous one.  Tables are ordered by lattice,
+// then row, so consecutive tiles touch neighbouring memory.
+#pragma once
+
+#include "lbm_fused_async.cuh"
+#include "lbm_fused_lean.cuh"
+#include "lbm_fused_sc.cuh"
+
+namespace lbm {
+
+struct BatchLattice {
+  LeanParams lean[2];   // [parity]
+  FusedParams full[2];  // [parity]
+  int flip;             // the lattice's parity at batch step parity 0
+};
+
+struct BatchTile {
+  int lat;
+  int item;
+};
+
+// the view of lattice `lat` at batch step parity `sp`
+__device__ __forceinline__ int view_of(const BatchLattice* lats, int lat, int sp) { return (sp ^ lats[lat].flip) & 1; }
+
+// word-wise copy of a trivially copyable struct by `n` cooperating threads
+template <typename T>
+__device__ __forceinline__ void copy_words(T* dst, const T* src, int tid, int n) {
+  static_assert(sizeof(T) % 4 == 0, "struct size must be a multiple of 4 bytes");
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  for (int i = tid; i < (int)(sizeof(T) / 4); i += n) d[i] = s[i];
+}
+
+constexpr int BATCH_WARPS = 8;  // warps per block of the segment kinds
+
+// Plain segments of every lattice in the table.
+template <int MODEL, bool PL, int ST, int V, int FORCE>
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLattice* __restrict__ lats,
+                                                                  const BatchTile* __restrict__ tiles, int ntiles,
+                                                                  int sp) {
+  __shared__ LeanParams lp[BATCH_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  LeanParams& p = lp[warp];
+  int cur = -1;
+  for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
+    const BatchTile tile = tiles[t];
+    if (tile.lat != cur) {
+      __syncwarp();
+      copy_words(&p, &lats[tile.lat].lean[view_of(lats, tile.lat, sp)], lane, 32);
+      __syncwarp();
+      cur = tile.lat;
+    }
+    const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
+    const int seg = tile.item - y * p.nseg;
+    const int x0s = seg * 32 * V, x0 = x0s + lane * V;
+    float h[V][9];
+    if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
+    else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
+    lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+  }
+}
+
+// Flagged segments (bounce-back links, boundary programs, saved moments,
+// inactive nodes) of every lattice in the table: the general path.
+template <int MODEL, bool PL, int ST, int V>
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_special(const BatchLattice* __restrict__ lats,
+                                                                     const BatchTile* __restrict__ tiles,
+                                                                     int ntiles, int sp) {
+  __shared__ FusedParams fp[BATCH_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FusedParams& p = fp[warp];
+  int cur = -1;
+  for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
+    const BatchTile tile = tiles[t];
+    if (tile.lat != cur) {
+      __syncwarp();
+      copy_words(&p, &lats[tile.lat].full[view_of(lats, tile.lat, sp)], lane, 32);
+      __syncwarp();
+      cur = tile.lat;
+    }
+    const int y = tile.item / p.nseg;
+    const int seg = tile.item - y * p.nseg;
+    const int x0 = seg * 32 * V + lane * V;
+    float f[V][9];
+    gather_direct<ST, V>(p, y, seg, lane, f);
+    fused_tail<MODEL, PL, ST, V>(p, f, y, seg, x0, x0 < p.nx);
+  }
+}
+
+// Shan-Chen tiles (item = ty + tiles_y * seg) of every lattice in the table.
+template <int MODEL, int ST, int V>
+__global__ void __launch_bounds__(SC_ROWS * 32) k_batch_sc(const BatchLattice* __restrict__ lats,
+                                                           const BatchTile* __restrict__ tiles, int ntiles, int sp) {
+  __shared__ FusedParams p;
+  __shared__ float psi[SC_ROWS + 2][32 * V + 2];
+  int cur = -1;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tile = tiles[t];  // uniform over the block
+    if (tile.lat != cur) {
+      __syncthreads();  // every warp is done with the previous parameters
+      copy_words(&p, &lats[tile.lat].full[view_of(lats, tile.lat, sp)], threadIdx.x, SC_ROWS * 32);
+      __syncthreads();
+      cur = tile.lat;
+    }
+    const int tiles_y = p.ny / SC_ROWS;
+    sc_tile<MODEL, ST, V>(p, tile.item % tiles_y, tile.item / tiles_y, psi);
+    __syncthreads();  // psi is rewritten by the next tile
+  }
+}
+
+// Drag/lift monitors: block b sums the momentum exchanged on monitor b's
+// solid links (lattice mon.lat, current post-collision state) and appends
+// (Fx, Fy) at series[2 * count], then advances count, so a graph replaying
+// the same launch fills consecutive rows.
+struct BatchMonitor {
+  int lat;
+  int64_t nlinks;
+  const int32_t* links;  // (site, k) pairs
+  double* series;        // [capacity][2]
+  int32_t* count;        // device counter
+  int32_t capacity;
+};
+
+template <int ST>
+__global__ void __launch_bounds__(MEX_TPB) k_batch_monitor(const BatchLattice* __restrict__ lats,
+                                                           const BatchMonitor* __restrict__ mons, int sp) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const BatchMonitor m = mons[blockIdx.x];
+  // the post-collision state written by this step is the view's destination
+  const FusedParams& p = lats[m.lat].full[view_of(lats, m.lat, sp)];
+  const T* src = reinterpret_cast<const T*>(p.dst);
+  double fx = 0.0, fy = 0.0;
+  for (int64_t i = threadIdx.x; i < m.nlinks; i += blockDim.x) {
+    const int64_t q = m.links[2 * i];
+    const int k = m.links[2 * i + 1];
+    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
+    fx += 2.0 * cx_dyn(k) * v;
+    fy += 2.0 * cy_dyn(k) * v;
+  }
+  __shared__ double sh[2][MEX_TPB / 32];
+  fx = warp_sum(fx);
+  fy = warp_sum(fy);
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = fx;
+    sh[1][threadIdx.x >> 5] = fy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sx = 0.0, sy = 0.0;
+    for (int i = 0; i < MEX_TPB / 32; ++i) {
+      sx += sh[0][i];
+      sy += sh[1][i];
+    }
+    const int c = *m.count;
+    if (c < m.capacity) {
+      m.series[2 * (size_t)c] = sx;
+      m.series[2 * (size_t)c + 1] = sy;
+    }
+    *m.count = c + 1;
+  }
+}
+
+// ------------------------------------------------------------ launchers
+// kind of a tile group
+enum { BATCH_LEAN = 0, BATCH_SC = 1, BATCH_SPECIAL = 2 };  // launch order within a step
+
+struct BatchGroup {
+  int kind, model, powerlaw, storage, V, force;
+  int offset, count;  // range in the tile table
+  int blocks;         // persistent grid (0 until first launch)
+};
+
+template <typename K>
+int batch_grid(K kern, int threads, int tiles_per_block, int count, int* blocks) {
+  if (!*blocks) {
+    int per_sm = 0, dev = 0, sms = 0;
+    int rc = lbm_err::cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0),
+                           "batch: occupancy");
+    if (!rc) rc = lbm_err::cuda(cudaGetDevice(&dev), "batch: device");
+    if (!rc) rc = lbm_err::cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "batch: SMs");
+    if (rc) return rc;
+    *blocks = (per_sm > 0 ? per_sm : 1) * sms;
+  }
+  const int need = (count + tiles_per_block - 1) / tiles_per_block;
+  return need < *blocks ? need : *blocks;
+}
+
+template <int MODEL, bool PL, int ST, int V>
+int launch_batch_seg(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
+  if (g.count == 0) return LBM_OK;
+  const BatchTile* t = tiles + g.offset;
+  if (g.kind == BATCH_SPECIAL) {
+    auto kern = k_batch_special<MODEL, PL, ST, V>;
+    const int b = batch_grid(kern, BATCH_WARPS * 32, BATCH_WARPS, g.count, &g.blocks);
+    if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
+    kern<<<b, BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
+    return lbm_err::launch("batched step (flagged segments)");
+  }
+  auto kern = g.force ? k_batch_lean<MODEL, PL, ST, V, 1> : k_batch_lean<MODEL, PL, ST, V, 0>;
+  const int b = batch_grid(kern, BATCH_WARPS * 32, BATCH_WARPS, g.count, &g.blocks);
+  if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
+  kern<<<b, BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
+  return lbm_err::launch("batched step (plain segments)");
+}
+
+template <int ST, int V>
+int launch_batch_v(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
+  switch (g.model * 2 + (g.powerlaw ? 1 : 0)) {
+    case 0: return launch_batch_seg<LBM_BGK, false, ST, V>(g, lats, tiles, sp, s);
+    case 1: return launch_batch_seg<LBM_BGK, true, ST, V>(g, lats, tiles, sp, s);
+    case 2: return launch_batch_seg<LBM_TRT, false, ST, V>(g, lats, tiles, sp, s);
+    case 3: return launch_batch_seg<LBM_TRT, true, ST, V>(g, lats, tiles, sp, s);
+    case 4: return launch_batch_seg<LBM_MRT, false, ST, V>(g, lats, tiles, sp, s);
+    case 5: return launch_batch_seg<LBM_MRT, true, ST, V>(g, lats, tiles, sp, s);
+    default: return lbm_err::set(LBM_ERR_ARG, "batch: collision model %d", g.model);
+  }
+}
+
+template <int ST>
+int launch_batch_sc(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
+  if (g.count == 0) return LBM_OK;
+  const BatchTile* t = tiles + g.offset;
+  auto kern = g.model == LBM_BGK ? k_batch_sc<LBM_BGK, ST, AV>
+                                 : (g.model == LBM_TRT ? k_batch_sc<LBM_TRT, ST, AV> : k_batch_sc<LBM_MRT, ST, AV>);
+  const int b = batch_grid(kern, SC_ROWS * 32, 1, g.count, &g.blocks);
+  if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
+  kern<<<b, SC_ROWS * 32, 0, s>>>(lats, t, g.count, sp);
+  return lbm_err::launch("batched Shan-Chen step");
+}
+
+// one group of storage ST for one step
+template <int ST>
+int launch_batch_group(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s);
+
+template <int ST>
+int launch_batch_monitors(const BatchLattice* lats, const BatchMonitor* mons, int nmon, int sp, cudaStream_t s) {
+  if (nmon == 0) return LBM_OK;
+  k_batch_monitor<ST><<<nmon, MEX_TPB, 0, s>>>(lats, mons, sp);
+  return lbm_err::launch("batched drag/lift monitors");
+}
+
+}  // namespace lbm
+
+#define LBM_BATCH_EXTERN(ST)                                                                                     \
+  namespace lbm {                                                                                                \
+  extern template int launch_batch_monitors<ST>(const BatchLattice*, const BatchMonitor*, int, int, cudaStream_t); \
+  }
+
+#define LBM_BATCH_INSTANTIATE(ST, VA, VB)                                                                       \
+  namespace lbm {                                                                                               \
+  template <>                                                                                                   \
+  int launch_batch_group<ST>(BatchGroup & g, const BatchLattice* lats, const BatchTile* tiles, int sp,          \
+                             cudaStream_t s) {                                                                  \
+    if (g.kind == BATCH_SC) return launch_batch_sc<ST>(g, lats, tiles, sp, s);                                  \
+    if (g.V == VA) return launch_batch_v<ST, VA>(g, lats, tiles, sp, s);                                        \
+    if (g.V == VB) return launch_batch_v<ST, VB>(g, lats, tiles, sp, s);                                        \
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch: nodes_per_thread %d not built for this storage", g.V);     \
+  }                                                                                                             \
+  template int launch_batch_monitors<ST>(const BatchLattice*, const BatchMonitor*, int, int, cudaStream_t);     \
+  }

@@ -62,6 +62,68 @@ struct FusedParams {
   float mwsh[9];    // MRT moments of the shift, M wsh
 };
 
+// The fields the lean (plain-segment) kernels read: a compact copy of
+// FusedParams that a batched kernel can stage per warp in shared memory.
+struct LeanParams {
+  int nx, ny, pitch, nseg;
+  size_t plane;
+  const void* src;
+  void* dst;
+  float* tau;
+  float omega, omega_a, magic, tau_min, tau_max, pl_m, pl_n;
+  float gx, gy;
+  float rho_shift;
+  uint32_t nseg_mul;  // item / nseg = (umulhi(item, nseg_mul) + item) >> nseg_shift
+  int nseg_shift;
+  float s[9];
+  float wsh[9];
+  float mwsh[9];
+};
+
+// Division by an invariant divisor d (1 <= d < 2^31) as a multiply-high and
+// shift (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994, round-up variant): l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(m, n) + n) >> l.
+inline void fast_div_setup(uint32_t d, uint32_t* mul, int* shift) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  *mul = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+  *shift = l;
+}
+__device__ __forceinline__ int fast_div(int n, uint32_t mul, int shift) {
+  const unsigned long long t = __umulhi((uint32_t)n, mul);
+  return (int)((t + (uint32_t)n) >> shift);
+}
+
+inline LeanParams lean_of(const FusedParams& f) {
+  LeanParams l;
+  l.nx = f.nx;
+  l.ny = f.ny;
+  l.pitch = f.pitch;
+  l.nseg = f.nseg;
+  l.plane = f.plane;
+  l.src = f.src;
+  l.dst = f.dst;
+  l.tau = f.tau;
+  l.omega = f.omega;
+  l.omega_a = f.omega_a;
+  l.magic = f.magic;
+  l.tau_min = f.tau_min;
+  l.tau_max = f.tau_max;
+  l.pl_m = f.pl_m;
+  l.pl_n = f.pl_n;
+  l.gx = f.gx;
+  l.gy = f.gy;
+  l.rho_shift = f.rho_shift;
+  fast_div_setup((uint32_t)f.nseg, &l.nseg_mul, &l.nseg_shift);
+  for (int a = 0; a < 9; ++a) {
+    l.s[a] = f.s[a];
+    l.wsh[a] = f.wsh[a];
+    l.mwsh[a] = f.mwsh[a];
+  }
+  return l;
+}
+
 // ------------------------------------------------------------ storage
 template <int ST>
 struct Storage;

@@ -135,8 +135,8 @@ __device__ __forceinline__ void store_raw(typename Storage<ST>::T* p, const floa
 // Pull gather of an interior segment (x0s > 0 and x0s + 32 V < nx): every
 // lane is inside the lattice, the elements across the segment's edges exist
 // without wrapping, and node nx-1 is not in the segment.
-template <int ST, int V>
-__device__ __forceinline__ void gather_interior(const FusedParams& p, int y, int x0, int lane, float (&h)[V][9]) {
+template <class P, int ST, int V>
+__device__ __forceinline__ void gather_interior(const P& p, int y, int x0, int lane, float (&h)[V][9]) {
   using T = typename Storage<ST>::T;
   constexpr unsigned FULL = 0xffffffffu;
   const T* src = reinterpret_cast<const T*>(p.src);
@@ -168,8 +168,8 @@ __device__ __forceinline__ void gather_interior(const FusedParams& p, int y, int
 
 // Pull gather of any segment (x edges wrap, lanes past nx read nothing),
 // stored values without the shift.
-template <int ST, int V>
-__device__ __forceinline__ void gather_edge(const FusedParams& p, int y, int x0, int lane, float (&h)[V][9]) {
+template <class P, int ST, int V>
+__device__ __forceinline__ void gather_edge(const P& p, int y, int x0, int lane, float (&h)[V][9]) {
   using T = typename Storage<ST>::T;
   constexpr unsigned FULL = 0xffffffffu;
   const bool live = x0 < p.nx;
@@ -216,8 +216,8 @@ __device__ __forceinline__ void gather_edge(const FusedParams& p, int y, int x0,
 // +- 3 w_k rho (c_k.u).
 // SCALED: every e_k is multiplied by sc (BGK passes omega, so that the
 // relaxation h + omega (e - h) becomes one fma, (1 - omega) h + omega e).
-template <bool SCALED = false>
-__device__ __forceinline__ void shifted_feq(const FusedParams& p, float rho, float ux, float uy, float e[9],
+template <bool SCALED = false, class P>
+__device__ __forceinline__ void shifted_feq(const P& p, float rho, float ux, float uy, float e[9],
                                             float sc = 1.0f) {
   const float base = fmaf(-1.5f, fmaf(ux, ux, uy * uy), 1.0f);
   const float rs = SCALED ? rho * sc : rho;
@@ -242,7 +242,7 @@ __device__ __forceinline__ void shifted_feq(const FusedParams& p, float rho, flo
 
 // Guo forcing populations F_k (CollisionEngine.py:21-25), by pairs
 __device__ __forceinline__ void pair_force(float Fx, float Fy, float ux, float uy, float F[9]) {
-  const float uF = ux * Fx + uy * Fy;
+  const float uF = fmaf(ux, Fx, uy * Fy);
   F[0] = W(0) * (-3.0f * uF);
   const float eu[4] = {ux, uy, ux + uy, uy - ux};
   const float eF[4] = {Fx, Fy, Fx + Fy, Fy - Fx};
@@ -251,26 +251,70 @@ __device__ __forceinline__ void pair_force(float Fx, float Fy, float ux, float u
     const int k = q < 2 ? q + 1 : q + 3;
     const float w = W(k);
     const float sym = w * fmaf(9.0f * eF[q], eu[q], -3.0f * uF);
-    const float anti = w * 3.0f * eF[q];
+    const float anti = (3.0f * w) * eF[q];
     F[k] = sym + anti;
     F[OPP(k)] = sym - anti;
   }
 }
 
+// The library is built without implicit fma contraction, so every kernel
+// form (single lattice, batched, prefetching) computes a node bit for bit
+// alike; the fused multiply-adds below are written out.
+__device__ __forceinline__ float shear_lean(const float n[9], float cof) {  // CollisionEngine.py:86-92
+  const float Sxx = (n[1] + n[3] + n[5] + n[6] + n[7] + n[8]) * cof;
+  const float Syy = (n[2] + n[4] + n[5] + n[6] + n[7] + n[8]) * cof;
+  const float Sxy = (n[5] - n[6] + n[7] - n[8]) * cof;
+  return sqrtf(2.0f * fmaf(Sxx, Sxx, fmaf(Syy, Syy, 2.0f * (Sxy * Sxy))));
+}
+__device__ __forceinline__ float powerlaw_tau_lean(float m, float n, float gamma, float lo, float hi) {
+  return clamp_tau(fmaf(m * powf(gamma, n - 1.0f), 3.0f, 0.5f), lo, hi);  // FluidModels.py:20-29
+}
+// MRT transforms (CollisionEngine.py:273-282): forward coefficients are
+// 0, +-1, +-2, +-4 (an fma by a power of two rounds as a multiply and add)
+__device__ __forceinline__ void mrt_forward_lean(const float f[9], float m[9]) {
+#pragma unroll
+  for (int a = 0; a < 9; ++a) {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      constexpr float one = 1.0f;
+      const float c = MRT_M(a, k);
+      if (c == one) s = s + f[k];
+      else if (c == -one) s = s - f[k];
+      else if (c != 0.0f) s = fmaf(c, f[k], s);
+    }
+    m[a] = s;
+  }
+}
+__device__ __forceinline__ void mrt_backward_lean(const float m[9], float f[9]) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 9; ++a)
+      if (MRT_M(a, k) != 0.0f) s = fmaf(MRT_MINV(k, a), m[a], s);
+    f[k] = s;
+  }
+}
+
 // One node: moments, relaxation and collision of the stored values h in
-// place; returns the new power-law state (or the old one).
-template <int MODEL, bool PL, int FORCE>
-__device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], float state) {
+// place; returns the new power-law state (or the old one).  FORCE: 0 none,
+// 1 the uniform body force (p.gx, p.gy), 2 the per-node force (Fn_x, Fn_y).
+template <class P, int MODEL, bool PL, int FORCE>
+__device__ __forceinline__ float collide_lean(const P& p, float h[9], float state, float Fn_x = 0.0f,
+                                              float Fn_y = 0.0f) {
   const float dr = ((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7])) + h[8];
   const float rho = dr + p.rho_shift;
-  const float jx = (h[1] - h[3]) + (h[5] - h[6]) + (h[8] - h[7]);
-  const float jy = (h[2] - h[4]) + (h[5] + h[6]) - (h[7] + h[8]);
-  const float Fx = FORCE == 1 ? p.gx : 0.0f, Fy = FORCE == 1 ? p.gy : 0.0f;
+  const float d13 = h[1] - h[3], d24 = h[2] - h[4], d57 = h[5] - h[7], d68 = h[6] - h[8];
+  const float jx = d13 + (d57 - d68);
+  const float jy = d24 + (d57 + d68);
+  const float Fx = FORCE == 1 ? p.gx : (FORCE == 2 ? Fn_x : 0.0f);
+  const float Fy = FORCE == 1 ? p.gy : (FORCE == 2 ? Fn_y : 0.0f);
   const float inv = __fdividef(1.0f, rho);  // within 2 ulp; rho is O(1) here
-  const float ux = (FORCE == 1 ? fmaf(0.5f, Fx, jx) : jx) * inv;
-  const float uy = (FORCE == 1 ? fmaf(0.5f, Fy, jy) : jy) * inv;
+  const float ux = (FORCE ? fmaf(0.5f, Fx, jx) : jx) * inv;
+  const float uy = (FORCE ? fmaf(0.5f, Fy, jy) : jy) * inv;
   float F[9];
-  if (FORCE == 1) pair_force(Fx, Fy, ux, uy, F);
+  if (FORCE) pair_force(Fx, Fy, ux, uy, F);
   if (MODEL == LBM_BGK && !PL) {
     // h' = (1 - omega) h + omega e (+ (1 - omega / 2) F)
     const float om = p.omega, keep = 1.0f - om, cf = 1.0f - 0.5f * om;
@@ -279,7 +323,7 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       float v = fmaf(keep, h[k], e[k]);
-      if (FORCE == 1) v = fmaf(cf, F[k], v);
+      if (FORCE) v = fmaf(cf, F[k], v);
       h[k] = v;
     }
     return state;
@@ -289,34 +333,56 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
 
   if (MODEL == LBM_MRT) {
     // m = M h; equilibrium moments less the moments of the shift (M wsh)
-    float n[9], m[9], meq[9], s[9];
+    float m[9], s[9];
 #pragma unroll
     for (int a = 0; a < 9; ++a) s[a] = p.s[a];
     if (PL) {
       // CollisionEngine.py:332-377 with the previous step's s7 = s8 = state
+      float n[9], mn[9], mneq[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) n[k] = h[k] - e[k];
-      float mn[9], mneq[9];
-      mrt_forward(n, mn);
+      mrt_forward_lean(n, mn);
       s[7] = s[8] = state;
 #pragma unroll
       for (int a = 0; a < 9; ++a) mn[a] *= s[a];
-      mrt_backward(mn, mneq);
-      const float gamma = shear_from_neq(mneq, -1.5f / rho);
-      state = 1.0f / powerlaw_tau(p.pl_m, p.pl_n, gamma, p.tau_min, p.tau_max);
+      mrt_backward_lean(mn, mneq);
+      const float gamma = shear_lean(mneq, -1.5f / rho);
+      state = 1.0f / powerlaw_tau_lean(p.pl_m, p.pl_n, gamma, p.tau_min, p.tau_max);
       s[7] = s[8] = state;
     }
-    mrt_forward(h, m);
-    mrt_meq(rho, ux, uy, meq);
+    mrt_forward_lean(h, m);
+    // equilibrium moments (CollisionEngine.py:388-406)
+    const float u2 = fmaf(ux, ux, uy * uy);
+    float meq[9];
+    meq[0] = rho;
+    meq[1] = rho * fmaf(3.0f, u2, -2.0f);
+    meq[2] = rho * fmaf(-3.0f, u2, 1.0f);
+    meq[3] = rho * ux;
+    meq[4] = -meq[3];
+    meq[5] = rho * uy;
+    meq[6] = -meq[5];
+    meq[7] = rho * fmaf(ux, ux, -(uy * uy));
+    meq[8] = rho * (ux * uy);
     float mf[9];
-    if (FORCE == 1) mrt_mforce(Fx, Fy, ux, uy, mf);
+    if (FORCE) {  // CollisionEngine.py:408-422
+      const float Fu = fmaf(Fx, ux, Fy * uy);
+      mf[0] = 0.0f;
+      mf[1] = 6.0f * Fu;
+      mf[2] = -6.0f * Fu;
+      mf[3] = Fx;
+      mf[4] = -Fx;
+      mf[5] = Fy;
+      mf[6] = -Fy;
+      mf[7] = 2.0f * fmaf(Fx, ux, -(Fy * uy));
+      mf[8] = fmaf(Fy, ux, Fx * uy);
+    }
 #pragma unroll
     for (int a = 0; a < 9; ++a) {
-      float v = m[a] - s[a] * (m[a] - (meq[a] - p.mwsh[a]));
-      if (FORCE == 1) v += (1.0f - 0.5f * s[a]) * mf[a];
+      float v = fmaf(-s[a], m[a] - (meq[a] - p.mwsh[a]), m[a]);
+      if (FORCE) v = fmaf(1.0f - 0.5f * s[a], mf[a], v);
       m[a] = v;
     }
-    mrt_backward(m, h);
+    mrt_backward_lean(m, h);
     return state;
   }
 
@@ -326,7 +392,7 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
     float n[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) n[k] = h[k] - e[k];
-    const float t = powerlaw_tau(p.pl_m, p.pl_n, shear_from_neq(n, -1.5f / rho / state), p.tau_min, p.tau_max);
+    const float t = powerlaw_tau_lean(p.pl_m, p.pl_n, shear_lean(n, -1.5f / rho / state), p.tau_min, p.tau_max);
     state = t;
     om = 1.0f / t;
     if (MODEL == LBM_TRT) oa = 1.0f / (p.magic / (t - 0.5f) + 0.5f);
@@ -336,35 +402,36 @@ __device__ __forceinline__ float collide_lean(const FusedParams& p, float h[9], 
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       float v = fmaf(om, e[k] - h[k], h[k]);
-      if (FORCE == 1) v = fmaf(cf, F[k], v);
+      if (FORCE) v = fmaf(cf, F[k], v);
       h[k] = v;
     }
     return state;
   }
-  // TRT, pairs (1,3), (2,4), (5,7), (6,8)
-  const float cs = 1.0f - 0.5f * om, ca = 1.0f - 0.5f * oa;
+  // TRT, pairs (1,3), (2,4), (5,7), (6,8): symmetric and antisymmetric parts
+  // relax with omega and omega_a (CollisionEngine.py:181-245)
+  const float hs = 0.5f * om, ha = 0.5f * oa;
+  const float cs = 0.5f * (1.0f - 0.5f * om), ca = 0.5f * (1.0f - 0.5f * oa);
   h[0] = fmaf(om, e[0] - h[0], h[0]);
-  if (FORCE == 1) h[0] = fmaf(cs, F[0], h[0]);
+  if (FORCE) h[0] = fmaf(1.0f - 0.5f * om, F[0], h[0]);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int k = q < 2 ? q + 1 : q + 3, o = OPP(k);
-    const float hs = 0.5f * (h[k] + h[o]), ha = 0.5f * (h[k] - h[o]);
-    const float es = 0.5f * (e[k] + e[o]), ea = 0.5f * (e[k] - e[o]);
-    float sym = om * (es - hs), anti = oa * (ea - ha);
-    if (FORCE == 1) {
-      sym = fmaf(cs, 0.5f * (F[k] + F[o]), sym);
-      anti = fmaf(ca, 0.5f * (F[k] - F[o]), anti);
+    float sym = hs * ((e[k] + e[o]) - (h[k] + h[o]));
+    float anti = ha * ((e[k] - e[o]) - (h[k] - h[o]));
+    if (FORCE) {
+      sym = fmaf(cs, F[k] + F[o], sym);
+      anti = fmaf(ca, F[k] - F[o], anti);
     }
-    h[k] = h[k] + sym + anti;
-    h[o] = h[o] + sym - anti;
+    h[k] = h[k] + (sym + anti);
+    h[o] = h[o] + (sym - anti);
   }
   return state;
 }
 
 // Moments, collision and stores of one lane's V nodes (x0.., row y) of a
 // plain segment, from the gathered stored values h.
-template <int MODEL, bool PL, int ST, int V, int FORCE>
-__device__ __forceinline__ void lean_collide_store(const FusedParams& p, float (&h)[V][9], int y, int x0) {
+template <class P, int MODEL, bool PL, int ST, int V, int FORCE>
+__device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9], int y, int x0) {
   using T = typename Storage<ST>::T;
   const bool live = x0 < p.nx;
   const size_t rowoff = (size_t)y * p.pitch;
@@ -379,7 +446,7 @@ __device__ __forceinline__ void lean_collide_store(const FusedParams& p, float (
   }
 #pragma unroll
   for (int i = 0; i < V; ++i) {
-    const float st = collide_lean<MODEL, PL, FORCE>(p, h[i], PL ? tau[i] : 0.0f);
+    const float st = collide_lean<P, MODEL, PL, FORCE>(p, h[i], PL ? tau[i] : 0.0f);
     if (PL) tau[i] = st;
   }
   if (!live) return;
@@ -413,10 +480,10 @@ __global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
   ldg_early(p.seg_flags + (size_t)y * p.nseg + seg, flag);
   const int x0s = seg * 32 * V, x0 = x0s + lane * V;
   float h[V][9];
-  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<ST, V>(p, y, x0, lane, h);
-  else gather_edge<ST, V>(p, y, x0, lane, h);
+  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<FusedParams, ST, V>(p, y, x0, lane, h);
+  else gather_edge<FusedParams, ST, V>(p, y, x0, lane, h);
   if (flag) return;  // uniform over the warp: k_fused_special owns this segment
-  lean_collide_store<MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+  lean_collide_store<FusedParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
 }
 
 // ------------------------------------------------------------ prefetching form
@@ -553,7 +620,7 @@ __device__ __forceinline__ void pf_consume(const FusedParams& p, const unsigned 
       }
     }
   }
-  lean_collide_store<MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+  lean_collide_store<FusedParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
 }
 
 // blocks per SM the ring's shared memory allows (at most 2048 threads): the

@@ -16,41 +16,44 @@
 // populations per lattice update.
 #pragma once
 
-#include "lbm_fused.cuh"
+#include "lbm_fused_lean.cuh"
 
 namespace lbm {
 
 constexpr int SC_ROWS = 8;  // rows per block = warps per block
 
-template <int V>
-__device__ __forceinline__ float density_of(const float (&f)[V][9], int i) {
-  return ((f[i][0] + f[i][1]) + (f[i][2] + f[i][3])) + ((f[i][4] + f[i][5]) + (f[i][6] + f[i][7])) + f[i][8];
+// Density of a node from its stored (shifted) values h: the pairwise sum of
+// collide_lean, so psi and the collision see the same rho.
+__device__ __forceinline__ float density_raw(const float h[9], float rho_shift) {
+  return (((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7])) + h[8]) + rho_shift;
 }
 
-// rho of one node (scalar periodic pull)
+// rho of one node (periodic pull of its nine stored values)
 template <int ST>
 __device__ __forceinline__ float density_at(const FusedParams& p, int x, int y) {
-  using S = Storage<ST>;
-  using T = typename S::T;
+  using T = typename Storage<ST>::T;
   const T* src = reinterpret_cast<const T*>(p.src);
-  float r = 0.0f;
+  float h[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k)
-    r += S::dec(load1(src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch + wrap(x - CX(k), p.nx)),
-                p.wsh[k]);
-  return r;
+    h[k] = raw_to_float<ST>(
+        load1(src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch + wrap(x - CX(k), p.nx)));
+  return density_raw(h, p.rho_shift);
 }
 
+template <int ST, int V>
+__device__ __forceinline__ void sc_gather(const FusedParams& p, int y, int x0s, int x0, int lane, float (&h)[V][9]) {
+  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<FusedParams, ST, V>(p, y, x0, lane, h);
+  else gather_edge<FusedParams, ST, V>(p, y, x0, lane, h);
+}
+
+// One tile (rows ty*SC_ROWS.., segment seg) by one block of SC_ROWS warps;
+// psi is the block's shared tile.  Ends with the block's last read of psi.
 template <int MODEL, int ST, int V>
-__global__ void __launch_bounds__(SC_ROWS * 32) k_fused_sc(const FusedParams p) {
-  using S = Storage<ST>;
-  using T = typename S::T;
+__device__ __forceinline__ void sc_tile(const FusedParams& p, int ty, int seg, float (&psi)[SC_ROWS + 2][32 * V + 2]) {
+  using T = typename Storage<ST>::T;
   constexpr int W_ = 32 * V;       // tile width
-  constexpr int PW = W_ + 2;       // psi row: columns x0s-1 .. x0s+W_
-  __shared__ float psi[SC_ROWS + 2][PW];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_y = p.ny / SC_ROWS;
-  const int ty = blockIdx.x % tiles_y, seg = blockIdx.x / tiles_y;
   const int y0 = ty * SC_ROWS, x0s = seg * W_;
   const int x0 = x0s + lane * V;
   const bool live = x0 < p.nx;
@@ -61,11 +64,11 @@ __global__ void __launch_bounds__(SC_ROWS * 32) k_fused_sc(const FusedParams p) 
   if (warp == 0 || warp == SC_ROWS - 1) {
     const int r = warp == 0 ? 0 : SC_ROWS + 1;
     const int yh = wrap(warp == 0 ? y0 - 1 : y0 + SC_ROWS, p.ny);
-    float h[V][9];
-    gather_direct<ST, V>(p, yh, seg, lane, h);
+    float hh[V][9];
+    sc_gather<ST, V>(p, yh, x0s, x0, lane, hh);
 #pragma unroll
     for (int i = 0; i < V; ++i)
-      if (lane * V + i < wlast) psi[r][1 + lane * V + i] = eos_psi(p.eos, density_of<V>(h, i), p.sc_T);
+      if (lane * V + i < wlast) psi[r][1 + lane * V + i] = eos_psi(p.eos, density_raw(hh[i], p.rho_shift), p.sc_T);
   }
   // column halos of all SC_ROWS + 2 rows: left = column x0s-1, right = the
   // column after the segment's last node (wraps to column 0 at the edge)
@@ -78,51 +81,43 @@ __global__ void __launch_bounds__(SC_ROWS * 32) k_fused_sc(const FusedParams p) 
   }
   // the warp's own row
   const int y = y0 + warp;
-  float f[V][9];
-  gather_direct<ST, V>(p, y, seg, lane, f);
-  float rho[V];
+  float h[V][9];
+  sc_gather<ST, V>(p, y, x0s, x0, lane, h);
 #pragma unroll
-  for (int i = 0; i < V; ++i) {
-    rho[i] = density_of<V>(f, i);
-    if (lane * V + i < wlast) psi[warp + 1][1 + lane * V + i] = eos_psi(p.eos, rho[i], p.sc_T);
-  }
+  for (int i = 0; i < V; ++i)
+    if (lane * V + i < wlast) psi[warp + 1][1 + lane * V + i] = eos_psi(p.eos, density_raw(h[i], p.rho_shift), p.sc_T);
   __syncthreads();
 
-  float s[9];
-#pragma unroll
-  for (int a = 0; a < 9; ++a) s[a] = p.s[a];
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     const int c = 1 + lane * V + i;
-    float Fx = 0.0f, Fy = 0.0f;
+    float Fx = 0.0f, Fy = 0.0f;  // sum_k w_k c_k psi(x + c_k)
 #pragma unroll
     for (int k = 1; k < 9; ++k) {
       const float ps = psi[warp + 1 + CY(k)][c + CX(k)];
-      Fx += W(k) * (float)CX(k) * ps;
-      Fy += W(k) * (float)CY(k) * ps;
+      if (CX(k) != 0) Fx = fmaf(W(k) * (float)CX(k), ps, Fx);
+      if (CY(k) != 0) Fy = fmaf(W(k) * (float)CY(k), ps, Fy);
     }
     const float m = -p.g_coh * psi[warp + 1][c];
-    Fx = Fx * m + p.gx;
-    Fy = Fy * m + p.gy;
-    float* fi = f[i];
-    const float r = rho[i];
-    const float jx = (fi[1] - fi[3]) + (fi[5] - fi[6]) + (fi[8] - fi[7]);
-    const float jy = (fi[2] - fi[4]) + (fi[5] + fi[6]) - (fi[7] + fi[8]);
-    const float ux = (jx + 0.5f * Fx) / r, uy = (jy + 0.5f * Fy) / r;
-    if (MODEL == LBM_BGK) collide_bgk(fi, r, ux, uy, Fx, Fy, p.omega, true);
-    else if (MODEL == LBM_TRT) collide_trt(fi, r, ux, uy, Fx, Fy, p.omega, p.omega_a, true);
-    else collide_mrt(fi, r, ux, uy, Fx, Fy, s, true);
+    collide_lean<FusedParams, MODEL, false, 2>(p, h[i], 0.0f, fmaf(Fx, m, p.gx), fmaf(Fy, m, p.gy));
   }
   if (!live) return;
   T* dst = reinterpret_cast<T*>(p.dst);
   const size_t rowoff = (size_t)y * p.pitch;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    T raw[V];
+    float v[V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], p.wsh[k]);
-    store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
+    for (int i = 0; i < V; ++i) v[i] = h[i][k];
+    store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, v);
   }
+}
+
+template <int MODEL, int ST, int V>
+__global__ void __launch_bounds__(SC_ROWS * 32) k_fused_sc(const FusedParams p) {
+  __shared__ float psi[SC_ROWS + 2][32 * V + 2];
+  const int tiles_y = p.ny / SC_ROWS;
+  sc_tile<MODEL, ST, V>(p, blockIdx.x % tiles_y, blockIdx.x / tiles_y, psi);
 }
 
 }  // namespace lbm

@@ -4,23 +4,11 @@
 #include <new>
 
 #include "lbm_fused_launch.cuh"
+#include "lbm_plan_internal.h"
 
 LBM_EXTERN_STORAGE(LBM_STORE_F32)
 LBM_EXTERN_STORAGE(LBM_STORE_F16S)
 LBM_EXTERN_STORAGE(LBM_STORE_BF16S)
-
-struct LbmPlan {
-  LbmPlanDesc d;
-  LbmPlanBuffers b;
-  bool bound = false;
-  int parity = 0;
-  lbm::FusedParams base;
-  // two-pass direct step: the flagged segments run on this plan-owned
-  // high-priority stream, forked from and joined back to the caller's stream
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
-  int side_dev = -1;
-};
 
 namespace {
 
@@ -30,7 +18,7 @@ int storage_bytes(int st) { return st == LBM_STORE_F32 ? 4 : 2; }
 
 bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
 
-FusedParams params_for(LbmPlan* pl) {
+FusedParams params_for(const LbmPlan* pl) {
   FusedParams p = pl->base;
   const int cur = pl->parity;
   p.src = cur ? pl->b.fb : pl->b.fa;
@@ -129,6 +117,8 @@ int step_once(LbmPlan* pl, cudaStream_t s) {
 }
 
 }  // namespace
+
+lbm::FusedParams lbm_plan_params(const LbmPlan* pl) { return params_for(pl); }
 
 extern "C" {
 

@@ -3,8 +3,8 @@
 Exports the reference package's public names (taichi_lbm/__init__.py of
 taichi-lbm) with the same constructors and methods; every per-step method is
 a CUDA kernel reached through the C ABI in include/lbm_gb300.h.  Additions:
-FusedSolver (the whole step as one kernel per time step) and
-UnsupportedComposition.
+FusedSolver (the whole step as one kernel per time step), Batch (many
+lattices advanced together) and UnsupportedComposition.
 """
 from . import _capi
 from .lbm import LBField, MacroscopicEngine
@@ -21,6 +21,7 @@ from .shanchen import (ShanChenForceC1, ShanChenForceC2, BoundaryEngineSC, OpenN
                        CS_psi)
 from .post import PostProcessingEngine
 from .solver import FusedSolver
+from .batch import Batch
 from ._plan import UnsupportedComposition
 
 _capi.load()

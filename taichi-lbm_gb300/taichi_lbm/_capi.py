@@ -127,6 +127,14 @@ _SIGS = {
     "lbm_reduce_scratch_doubles": ([], ctypes.c_int64),
     "lbm_plan_reduce_moments_noalloc": ([_vp, _vp, _vp], ctypes.c_int),
     "lbm_plan_reduce_moments": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "lbm_batch_create": ([_vp], ctypes.c_int),
+    "lbm_batch_add": ([_vp, _vp, _vp], ctypes.c_int),
+    "lbm_batch_remove": ([_vp, ctypes.c_int32], ctypes.c_int),
+    "lbm_batch_monitor": ([_vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int32], ctypes.c_int),
+    "lbm_batch_set_graph": ([_vp, ctypes.c_int32], ctypes.c_int),
+    "lbm_batch_run": ([_vp, ctypes.c_int32, _vp], ctypes.c_int),
+    "lbm_batch_info": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "lbm_batch_destroy": ([_vp], ctypes.c_int),
 }
 
 EXPORTED = tuple(_SIGS)

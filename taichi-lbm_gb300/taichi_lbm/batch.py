@@ -1,0 +1,87 @@
+"""Many lattices advanced together: a thin owner of an LbmBatch (C ABI).
+
+A member is a FusedSolver whose state is live on the device (begin() has
+run: the first step is done with the per-stage kernels, exactly as
+FusedSolver.step does).  Batch.run(n) then advances every member n steps,
+one persistent launch per kernel group per step (see lbm_batch_run in
+lbm_gb300.h); FusedSolver.finish() ends a member's run as usual.  So for one
+solver, ``begin(); batch.run(n - 1); finish()`` is ``step(n)``.
+
+Drag/lift monitors: ``add(solver, monitor_steps=m)`` records the momentum
+exchanged on the member's solid links after its first step and after every
+batched step, up to m rows; ``forces(slot)`` returns them as an (rows, 2)
+float64 CUDA tensor, the series FusedSolver.step(n, forces=True) returns.
+"""
+import ctypes
+
+import torch
+
+from . import _capi as A
+from .lbm import stream_handle
+
+
+class Batch:
+    def __init__(self, graphs=True):
+        h = ctypes.c_void_p()
+        A.call("lbm_batch_create", ctypes.byref(h))
+        self._h = h
+        self.graphs = bool(graphs)
+        A.call("lbm_batch_set_graph", self._h, 1 if self.graphs else 0)
+        self.members = {}  # slot -> (solver, monitor tensors or None)
+
+    def add(self, solver, monitor_steps=0):
+        """Join `solver` (beginning its run if needed); returns its slot."""
+        if not getattr(solver, "_live", False):
+            solver.begin()
+        mon = None
+        if monitor_steps:
+            links = solver.solid_links()
+            series = torch.zeros((int(monitor_steps), 2), dtype=torch.float64, device=solver.lb.device)
+            count = torch.ones(1, dtype=torch.int32, device=solver.lb.device)
+            # row 0: after the first step (the staged one)
+            A.call("lbm_plan_momentum_exchange", solver._plan, ctypes.c_void_p(links.data_ptr()),
+                   links.shape[0], ctypes.c_void_p(series.data_ptr()), stream_handle())
+            mon = (links, series, count)
+        slot = ctypes.c_int32()
+        A.call("lbm_batch_add", self._h, solver._plan, ctypes.byref(slot))
+        if mon is not None:
+            links, series, count = mon
+            A.call("lbm_batch_monitor", self._h, slot.value, ctypes.c_void_p(links.data_ptr()),
+                   links.shape[0], ctypes.c_void_p(series.data_ptr()), ctypes.c_void_p(count.data_ptr()),
+                   series.shape[0])
+        self.members[slot.value] = (solver, mon)
+        return slot.value
+
+    def remove(self, slot):
+        """Leave the batch; returns the solver (its state stays live)."""
+        A.call("lbm_batch_remove", self._h, int(slot))
+        solver, _ = self.members.pop(int(slot))
+        return solver
+
+    def run(self, nsteps):
+        A.call("lbm_batch_run", self._h, int(nsteps), stream_handle())
+
+    def forces(self, slot):
+        """(rows recorded, 2) float64 drag/lift series of a monitored member."""
+        _, mon = self.members[int(slot)]
+        if mon is None:
+            raise ValueError(f"member {slot} has no monitor")
+        _, series, count = mon
+        n = min(int(count.item()), series.shape[0])
+        return series[:n]
+
+    def info(self):
+        m, t, g = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        A.call("lbm_batch_info", self._h, ctypes.byref(m), ctypes.byref(t), ctypes.byref(g))
+        return {"members": m.value, "tiles": t.value, "groups": g.value}
+
+    def close(self):
+        if self._h is not None:
+            A.load().lbm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
