@@ -247,7 +247,7 @@ typedef struct LbmPlanDesc {
   /* Single-component Shan-Chen (ExternalForce.py:122-158) on a fully periodic
    * lattice: each step computes psi(rho, T) from the post-stream populations,
    * F = -g_coh psi(x) sum_k w_k c_k psi(x + c_k) + gravity, then collides.
-   * Needs the direct pipeline, nodes_per_thread 4, ny divisible by 8, no
+   * Needs the direct pipeline, nodes_per_thread 4, no
    * rewrite boundaries and a uniform temperature.                          */
   int32_t sc;
   float g_coh;

@@ -171,9 +171,8 @@ int rebuild(LbmBatch* b) {
     const int pw = pl->d.fluid_model == LBM_POWERLAW ? 1 : 0;
     if (pl->d.sc) {
       auto& t = bucket({lbm::BATCH_SC, pl->d.model, 0, pl->d.storage, pl->d.nodes_per_thread, 1});
-      const int tiles_y = p.ny / lbm::SC_ROWS;
-      for (int ty = 0; ty < tiles_y; ++ty)
-        for (int seg = 0; seg < p.nseg; ++seg) t.push_back({lat, ty + tiles_y * seg});
+      const int chunks = (p.ny + lbm::SC_CHUNK - 1) / lbm::SC_CHUNK;
+      for (int item = 0; item < chunks * p.nseg; ++item) t.push_back({lat, item});
     } else {
       flags.resize((size_t)p.ny * p.nseg);
       rc = lbm_err::cuda(cudaMemcpy(flags.data(), pl->b.seg_flags, flags.size(), cudaMemcpyDeviceToHost),

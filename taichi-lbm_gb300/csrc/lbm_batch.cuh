@@ -5,16 +5,14 @@
 // populations and saved moments read from / written to, for the two
 // ping-pong parities).  A tile is (lattice, item): for the plain and flagged
 // kinds an item is one row segment (y * nseg + seg), for Shan-Chen one
-// SC_ROWS x 32V block tile.  The kernels are persistent: a grid sized to the
-// GPU walks the table, a warp (or, for Shan-Chen, a block) per tile, and
-// copies a lattice's parameters into shared memory when its tile belongs to
-// another lattice than the previous one.  Tables are ordered by lattice,
+// strip of 32V columns and SC_CHUNK rows (chunk * nseg + seg).  The kernels
+// are persistent: a grid sized to the GPU walks the table, a warp per tile,
+// and copies a lattice's parameters into the warp's shared memory when its
+// tile belongs to another lattice than the previous one.  Tables are ordered by lattice,
 // then row, so consecutive tiles touch neighbouring memory.
 #pragma once
 
-#include "lbm_fused_async.cuh"
-#include "lbm_fused_lean.cuh"
-#include "lbm_fused_sc.cuh"
+#include "lbm_fused_launch.cuh"
 
 namespace lbm {
 
@@ -31,15 +29,6 @@ struct BatchTile {
 
 // the view of lattice `lat` at batch step parity `sp`
 __device__ __forceinline__ int view_of(const BatchLattice* lats, int lat, int sp) { return (sp ^ lats[lat].flip) & 1; }
-
-// word-wise copy of a trivially copyable struct by `n` cooperating threads
-template <typename T>
-__device__ __forceinline__ void copy_words(T* dst, const T* src, int tid, int n) {
-  static_assert(sizeof(T) % 4 == 0, "struct size must be a multiple of 4 bytes");
-  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-  for (int i = tid; i < (int)(sizeof(T) / 4); i += n) d[i] = s[i];
-}
 
 constexpr int BATCH_WARPS = 8;  // warps per block of the segment kinds
 
@@ -97,24 +86,28 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_special(const BatchL
   }
 }
 
-// Shan-Chen tiles (item = ty + tiles_y * seg) of every lattice in the table.
+// Shan-Chen strips (item = chunk * nseg + seg) of every lattice in the
+// table, one warp per strip.
 template <int MODEL, int ST, int V>
-__global__ void __launch_bounds__(SC_ROWS * 32) k_batch_sc(const BatchLattice* __restrict__ lats,
-                                                           const BatchTile* __restrict__ tiles, int ntiles, int sp) {
-  __shared__ FusedParams p;
-  __shared__ float psi[SC_ROWS + 2][32 * V + 2];
+__global__ void __launch_bounds__(SC_WARPS * 32) k_batch_sc(const BatchLattice* __restrict__ lats,
+                                                                const BatchTile* __restrict__ tiles, int ntiles,
+                                                                int sp) {
+  __shared__ LeanParams lp[SC_WARPS];
+  extern __shared__ __align__(16) unsigned char sc_ring[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  LeanParams& p = lp[warp];
+  unsigned char* ring = sc_ring + warp * sc_warp_bytes<ST, V>();
   int cur = -1;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const BatchTile tile = tiles[t];  // uniform over the block
+  for (int t = blockIdx.x * SC_WARPS + warp; t < ntiles; t += gridDim.x * SC_WARPS) {
+    const BatchTile tile = tiles[t];
     if (tile.lat != cur) {
-      __syncthreads();  // every warp is done with the previous parameters
-      copy_words(&p, &lats[tile.lat].full[view_of(lats, tile.lat, sp)], threadIdx.x, SC_ROWS * 32);
-      __syncthreads();
+      __syncwarp();
+      copy_words(&p, &lats[tile.lat].lean[view_of(lats, tile.lat, sp)], lane, 32);
+      __syncwarp();
       cur = tile.lat;
     }
-    const int tiles_y = p.ny / SC_ROWS;
-    sc_tile<MODEL, ST, V>(p, tile.item % tiles_y, tile.item / tiles_y, psi);
-    __syncthreads();  // psi is rewritten by the next tile
+    const int chunk = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
+    sc_strip<LeanParams, MODEL, ST, V>(p, tile.item - chunk * p.nseg, chunk, p.sc_rows, lane, ring);
   }
 }
 
@@ -233,9 +226,13 @@ int launch_batch_sc(BatchGroup& g, const BatchLattice* lats, const BatchTile* ti
   const BatchTile* t = tiles + g.offset;
   auto kern = g.model == LBM_BGK ? k_batch_sc<LBM_BGK, ST, AV>
                                  : (g.model == LBM_TRT ? k_batch_sc<LBM_TRT, ST, AV> : k_batch_sc<LBM_MRT, ST, AV>);
-  const int b = batch_grid(kern, SC_ROWS * 32, 1, g.count, &g.blocks);
-  if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
-  kern<<<b, SC_ROWS * 32, 0, s>>>(lats, t, g.count, sp);
+  const int smem = SC_WARPS * sc_warp_bytes<ST, AV>();
+  if (!g.blocks) {
+    int rc = persistent_blocks(kern, SC_WARPS * 32, smem, &g.blocks);
+    if (rc) return rc;
+  }
+  const int need = (g.count + SC_WARPS - 1) / SC_WARPS;
+  kern<<<need < g.blocks ? need : g.blocks, SC_WARPS * 32, smem, s>>>(lats, t, g.count, sp);
   return lbm_err::launch("batched Shan-Chen step");
 }
 

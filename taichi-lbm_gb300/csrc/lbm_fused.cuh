@@ -78,6 +78,10 @@ struct LeanParams {
   float s[9];
   float wsh[9];
   float mwsh[9];
+  // single-component Shan-Chen
+  float g_coh, sc_T;
+  LbmEos eos;
+  int sc_rows;  // rows of a strip item
 };
 
 // Division by an invariant divisor d (1 <= d < 2^31) as a multiply-high and
@@ -121,7 +125,20 @@ inline LeanParams lean_of(const FusedParams& f) {
     l.wsh[a] = f.wsh[a];
     l.mwsh[a] = f.mwsh[a];
   }
+  l.g_coh = f.g_coh;
+  l.sc_T = f.sc_T;
+  l.eos = f.eos;
+  l.sc_rows = 16;
   return l;
+}
+
+// word-wise copy of a trivially copyable struct by `n` cooperating threads
+template <typename T>
+__device__ __forceinline__ void copy_words(T* dst, const T* src, int tid, int n) {
+  static_assert(sizeof(T) % 4 == 0, "struct size must be a multiple of 4 bytes");
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  for (int i = tid; i < (int)(sizeof(T) / 4); i += n) d[i] = s[i];
 }
 
 // ------------------------------------------------------------ storage

@@ -9,18 +9,6 @@
 
 namespace lbm {
 
-template <int ST>
-int launch_fused_sc(const FusedParams& p, cudaStream_t s) {
-  const unsigned blocks = (unsigned)((p.ny / SC_ROWS) * p.nseg);
-  switch (p.model) {
-    case LBM_BGK: k_fused_sc<LBM_BGK, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
-    case LBM_TRT: k_fused_sc<LBM_TRT, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
-    case LBM_MRT: k_fused_sc<LBM_MRT, ST, AV><<<blocks, SC_ROWS * 32, 0, s>>>(p); break;
-    default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", p.model);
-  }
-  return lbm_err::launch("fused Shan-Chen step");
-}
-
 // Grid of a persistent kernel: as many blocks as fit on every SM.
 template <typename K>
 int persistent_blocks(K kern, int threads, int smem, int* blocks) {
@@ -40,6 +28,32 @@ int persistent_blocks(K kern, int threads, int smem, int* blocks) {
   if (rc) return rc;
   *blocks = (per_sm > 0 ? per_sm : 1) * sms;
   return LBM_OK;
+}
+
+// Shan-Chen strips of one lattice: persistent grid of warps, one strip each
+template <int MODEL, int ST>
+int launch_sc_model(LeanParams p, cudaStream_t s) {
+  static int blocks = 0;
+  auto kern = k_fused_sc<MODEL, ST, AV>;
+  const int smem = SC_WARPS * sc_warp_bytes<ST, AV>();
+  int rc = persistent_blocks(kern, SC_WARPS * 32, smem, &blocks);
+  if (rc) return rc;
+  p.sc_rows = sc_rows(p.ny, p.nseg, 2 * blocks * SC_WARPS);
+  const int nitems = p.nseg * ((p.ny + p.sc_rows - 1) / p.sc_rows);
+  const int need = (nitems + SC_WARPS - 1) / SC_WARPS;
+  kern<<<need < blocks ? need : blocks, SC_WARPS * 32, smem, s>>>(p, nitems);
+  return lbm_err::launch("fused Shan-Chen step");
+}
+
+template <int ST>
+int launch_fused_sc(const FusedParams& fp, cudaStream_t s) {
+  const LeanParams p = lean_of(fp);
+  switch (fp.model) {
+    case LBM_BGK: return launch_sc_model<LBM_BGK, ST>(p, s);
+    case LBM_TRT: return launch_sc_model<LBM_TRT, ST>(p, s);
+    case LBM_MRT: return launch_sc_model<LBM_MRT, ST>(p, s);
+    default: return lbm_err::set(LBM_ERR_ARG, "unknown collision model %d", fp.model);
+  }
 }
 
 template <int MODEL, bool PL, int ST, int NW, int NS>

@@ -544,47 +544,45 @@ __device__ __forceinline__ float edge_value(uint32_t w, int x) {
   }
 }
 
-template <int ST, int V, int NS>
-__device__ __forceinline__ void pf_issue(const FusedParams& p, unsigned char* stage, int item, int lane) {
+// Issue the cp.async copies of what row y of the segment at x0s needs from
+// the source into a stage (no commit): every lane's V elements of the nine
+// pulled rows and the 4-byte words holding the elements across the
+// segment's edges.
+template <class P, int ST, int V, int NS>
+__device__ __forceinline__ void stage_issue_row(const P& p, unsigned char* stage, int y, int x0s, int lane) {
   using T = typename Storage<ST>::T;
   using G = PfGeom<ST, V, NS>;
-  if (item >= 0) {
-    const int y = item / p.nseg;
-    const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
-    const bool live = x0 < p.nx;
-    const int ilast = p.nx - 1 - x0;
-    const bool need_right = live && (lane == 31 || (ilast >= 0 && ilast < V));
-    const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
-    const int xr = x0 + V < p.nx ? x0 + V : 0;
-    const T* src = reinterpret_cast<const T*>(p.src);
-    uint32_t* edges = reinterpret_cast<uint32_t*>(stage + G::EDGE_OFF);
+  const int x0 = x0s + lane * V;
+  const bool live = x0 < p.nx;
+  const int ilast = p.nx - 1 - x0;
+  const bool need_right = live && (lane == 31 || (ilast >= 0 && ilast < V));
+  const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
+  const int xr = x0 + V < p.nx ? x0 + V : 0;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  uint32_t* edges = reinterpret_cast<uint32_t*>(stage + G::EDGE_OFF);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
-      if (live) cp_async<V * (int)sizeof(T)>(stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), row + x0);
-      if (CX(k) == 1 && lane == 0 && live) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xl));
-      if (CX(k) == -1 && need_right) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xr));
-    }
-    reinterpret_cast<int*>(stage + G::ITEM_OFF)[lane] = item;
+  for (int k = 0; k < 9; ++k) {
+    const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
+    if (live) cp_async<V * (int)sizeof(T)>(stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), row + x0);
+    if (CX(k) == 1 && lane == 0 && live) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xl));
+    if (CX(k) == -1 && need_right) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xr));
   }
-  cp_async_commit();
 }
 
-template <int MODEL, bool PL, int ST, int V, int FORCE, int NS>
-__device__ __forceinline__ void pf_consume(const FusedParams& p, const unsigned char* stage, int lane) {
+// The pull gather of a row from its stage (after its copies have landed;
+// each lane reads only what it copied).
+template <class P, int ST, int V, int NS>
+__device__ __forceinline__ void stage_gather_row(const P& p, const unsigned char* stage, int x0, int lane,
+                                                 float (&h)[V][9]) {
   using T = typename Storage<ST>::T;
   using G = PfGeom<ST, V, NS>;
   constexpr unsigned FULL = 0xffffffffu;
-  const int item = reinterpret_cast<const int*>(stage + G::ITEM_OFF)[lane];
-  const int y = item / p.nseg;
-  const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
   const bool live = x0 < p.nx;
   const int ilast = p.nx - 1 - x0;
   const bool has_last = ilast >= 0 && ilast < V;
   const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
   const int xr = x0 + V < p.nx ? x0 + V : 0;
   const uint32_t* edges = reinterpret_cast<const uint32_t*>(stage + G::EDGE_OFF);
-  float h[V][9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     float c[V];
@@ -620,6 +618,27 @@ __device__ __forceinline__ void pf_consume(const FusedParams& p, const unsigned 
       }
     }
   }
+}
+
+template <int ST, int V, int NS>
+__device__ __forceinline__ void pf_issue(const FusedParams& p, unsigned char* stage, int item, int lane) {
+  using G = PfGeom<ST, V, NS>;
+  if (item >= 0) {
+    const int y = item / p.nseg;
+    stage_issue_row<FusedParams, ST, V, NS>(p, stage, y, (item - y * p.nseg) * 32 * V, lane);
+    reinterpret_cast<int*>(stage + G::ITEM_OFF)[lane] = item;
+  }
+  cp_async_commit();
+}
+
+template <int MODEL, bool PL, int ST, int V, int FORCE, int NS>
+__device__ __forceinline__ void pf_consume(const FusedParams& p, const unsigned char* stage, int lane) {
+  using G = PfGeom<ST, V, NS>;
+  const int item = reinterpret_cast<const int*>(stage + G::ITEM_OFF)[lane];
+  const int y = item / p.nseg;
+  const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
+  float h[V][9];
+  stage_gather_row<FusedParams, ST, V, NS>(p, stage, x0, lane, h);
   lean_collide_store<FusedParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
 }
 

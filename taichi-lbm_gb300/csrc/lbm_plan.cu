@@ -151,8 +151,6 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
                           lbm::AV);
     if (d->fluid_model != LBM_NEWTONIAN || d->nbc != 0)
       return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans take no power law and no rewrite boundaries");
-    if (d->ny % lbm::SC_ROWS)
-      return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans need ny divisible by %d", lbm::SC_ROWS);
   }
   if (d->nbc < 0 || d->nbc > LBM_MAX_BC) return lbm_err::set(LBM_ERR_ARG, "nbc %d", d->nbc);
   if (d->nprog < 0 || d->nprog > LBM_MAX_PROG) return lbm_err::set(LBM_ERR_ARG, "nprog %d", d->nprog);

@@ -62,9 +62,8 @@ class FusedSolver:
             if kinds != {PeriodicPsi_LR, PeriodicPsi_BT}:
                 raise UnsupportedComposition("the fused Shan-Chen step needs the psi boundaries "
                                              "PeriodicPsi_LR and PeriodicPsi_BT (a periodic lattice)")
-            if pipeline != "direct" or lb_field.NY % 8:
-                raise UnsupportedComposition("the fused Shan-Chen step runs the direct pipeline on "
-                                             "lattices with NY divisible by 8")
+            if pipeline != "direct":
+                raise UnsupportedComposition("the fused Shan-Chen step runs the direct pipeline")
         self.lb = lb_field
         self.me = macroscopic_engine
         self.coll = collision

@@ -132,3 +132,22 @@ def shan_chen_box(tl, nx, ny, psi, g_coh, T, rho_init, model="bgk", tau=1.0, mag
     lb.vel.fill([0.0, 0.0])
     lb.init_LBM(coll, fluid.group)
     return lb, me, coll, be, sc, bsc
+
+
+def batched_shan_chen(tl, count=64, sides=tuple(range(128, 1025, 64)), seed=20261203, tt_range=(0.7, 0.9),
+                      g_coh=-1.0, tau=1.0, model="bgk", keep_init=False):
+    """Many independent periodic Shan-Chen lattices of uneven sizes: side L
+    drawn uniformly from `sides`, Carnahan-Starling EOS (a=1, b=4, R=1) at
+    T/Tc ~ U[tt_range], rho0 = 0.25 (1 + U[-0.01, 0.01]), all from one seeded
+    numpy PCG64 generator.  Returns a list of (lb, me, coll, be, sc, bsc)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = rng.choice(np.asarray(sides), size=count)
+    tt = rng.uniform(tt_range[0], tt_range[1], size=count)
+    out = []
+    for n in range(count):
+        side = int(L[n])
+        psi, T = carnahan_starling(tl, float(tt[n]))
+        rho0 = 0.25 * (1.0 + rng.uniform(-0.01, 0.01, size=(side, side)))
+        out.append(shan_chen_box(tl, side, side, psi, g_coh, T, rho0, model=model, tau=tau,
+                                 name=f"sc{n}", keep_init=keep_init))
+    return out
