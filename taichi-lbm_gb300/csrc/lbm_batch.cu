@@ -150,6 +150,16 @@ int rebuild(LbmBatch* b) {
   auto bucket = [&](const GroupKey& k) -> std::vector<BatchTile>& { return by_key[k]; };
   std::vector<BatchMonitor> mons[3];
   std::vector<uint8_t> flags;
+  // rows per Shan-Chen strip: the longest that still gives the GPU enough
+  // strips in total (two per resident warp of 152 SMs x 12 warps)
+  int sc_rows = 2 * lbm::SC_CHUNK;
+  for (; sc_rows > lbm::SC_CHUNK / 2; sc_rows /= 2) {
+    long long items = 0;
+    for (const BatchMember& m : b->slots)
+      if (m.plan && m.plan->d.sc)
+        items += (long long)m.plan->base.nseg * ((m.plan->d.ny + sc_rows - 1) / sc_rows);
+    if (items >= 2 * 152 * 12) break;
+  }
   for (BatchMember& m : b->slots) {
     if (!m.plan) continue;
     LbmPlan* pl = m.plan;
@@ -163,6 +173,7 @@ int rebuild(LbmBatch* b) {
       rec.full[v].special = nullptr;  // the batch supplies its own tiles
       rec.full[v].plain = nullptr;
       rec.lean[v] = lbm::lean_of(rec.full[v]);
+      rec.lean[v].sc_rows = sc_rows;
     }
     pl->parity = saved;
     rec.flip = saved ^ sp;
@@ -171,7 +182,7 @@ int rebuild(LbmBatch* b) {
     const int pw = pl->d.fluid_model == LBM_POWERLAW ? 1 : 0;
     if (pl->d.sc) {
       auto& t = bucket({lbm::BATCH_SC, pl->d.model, 0, pl->d.storage, pl->d.nodes_per_thread, 1});
-      const int chunks = (p.ny + lbm::SC_CHUNK - 1) / lbm::SC_CHUNK;
+      const int chunks = (p.ny + sc_rows - 1) / sc_rows;
       for (int item = 0; item < chunks * p.nseg; ++item) t.push_back({lat, item});
     } else {
       flags.resize((size_t)p.ny * p.nseg);

@@ -135,12 +135,22 @@ __device__ __forceinline__ void sc_issue(const P& p, unsigned char* ring, int j,
 // psi of row y from its stage: the lane's V nodes and the two halo columns
 // (their nine populations summed by a shuffle tree in the pairwise order of
 // density_raw, so a column's psi is the same in every strip that needs it)
+// The pulled values replace the copied ones in the stage (each lane its own
+// V per population), so the collision reads them back without the gather.
 template <class P, int ST, int V>
-__device__ __forceinline__ void sc_stage_psi(const P& p, const unsigned char* st, int x0s, int lane, ScRow<V>& r) {
+__device__ __forceinline__ void sc_stage_psi(const P& p, unsigned char* st, int x0s, int lane, ScRow<V>& r) {
+  using T = typename Storage<ST>::T;
   using G = ScGeom<ST, V>;
   constexpr unsigned FULL = 0xffffffffu;
   float h[V][9];
   stage_gather_row<P, ST, V, sc_slots<ST>()>(p, st, x0s + lane * V, lane, h);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    T raw[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) raw[i] = T(h[i][k]);  // exact: h holds stored values
+    memcpy(st + k * G::POP_BYTES + lane * V * (int)sizeof(T), raw, sizeof(raw));
+  }
   int k;
   const int xs = sc_halo_column<P, V>(p, x0s, lane, k);
   const float v = xs >= 0 ? edge_value<ST>(reinterpret_cast<const uint32_t*>(st + G::ITEM_OFF)[lane], xs) : 0.0f;
@@ -194,8 +204,16 @@ __device__ __forceinline__ void sc_stage_collide(const P& p, const unsigned char
     Fx[i] = fmaf(fx, mm, p.gx);
     Fy[i] = fmaf(fy, mm, p.gy);
   }
-  float h[V][9];
-  stage_gather_row<P, ST, V, sc_slots<ST>()>(p, st, x0, lane, h);
+  float h[V][9];  // the pulled values sc_stage_psi left in the stage
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    T raw[V];
+    memcpy(raw, st + k * ScGeom<ST, V>::POP_BYTES + lane * V * (int)sizeof(T), sizeof(raw));
+    float c[V];
+    raw_to_floats<ST, V>(raw, c);
+#pragma unroll
+    for (int i = 0; i < V; ++i) h[i][k] = c[i];
+  }
 #pragma unroll
   for (int i = 0; i < V; ++i) collide_lean<P, MODEL, false, 2>(p, h[i], 0.0f, Fx[i], Fy[i]);
   if (x0 >= p.nx) return;
@@ -237,11 +255,12 @@ __device__ __forceinline__ void sc_strip(const P& p, int seg, int chunk, int row
   cp_async_wait<0>();
 }
 
-// rows per strip item: SC_CHUNK, halved while the lattice offers fewer than
-// `want` items (the extra rows per item are two, so shorter strips cost more)
+// rows per strip item: 2 SC_CHUNK, halved (down to SC_CHUNK / 2) while the
+// lattice offers fewer than `want` items (the extra rows per item are two,
+// so shorter strips cost more)
 inline int sc_rows(int ny, int nseg, int want) {
-  int r = SC_CHUNK;
-  while (r > 8 && (long long)nseg * ((ny + r - 1) / r) < want) r /= 2;
+  int r = 2 * SC_CHUNK;
+  while (r > SC_CHUNK / 2 && (long long)nseg * ((ny + r - 1) / r) < want) r /= 2;
   return r;
 }
 

@@ -22,6 +22,7 @@ from .shanchen import (ShanChenForceC1, ShanChenForceC2, BoundaryEngineSC, OpenN
 from .post import PostProcessingEngine
 from .solver import FusedSolver
 from .batch import Batch
+from .serving import Request, Server
 from ._plan import UnsupportedComposition
 
 _capi.load()

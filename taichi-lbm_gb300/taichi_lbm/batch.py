@@ -29,19 +29,27 @@ class Batch:
         A.call("lbm_batch_set_graph", self._h, 1 if self.graphs else 0)
         self.members = {}  # slot -> (solver, monitor tensors or None)
 
-    def add(self, solver, monitor_steps=0):
-        """Join `solver` (beginning its run if needed); returns its slot."""
+    @staticmethod
+    def prepare(solver, monitor_steps=0):
+        """Begin `solver`'s run if needed and, for monitor_steps > 0, record its
+        first-step drag/lift row; returns the monitor tensors (or None) for
+        add().  Runs on the current stream, so a builder thread may prepare
+        members on its own stream."""
         if not getattr(solver, "_live", False):
             solver.begin()
-        mon = None
-        if monitor_steps:
-            links = solver.solid_links()
-            series = torch.zeros((int(monitor_steps), 2), dtype=torch.float64, device=solver.lb.device)
-            count = torch.ones(1, dtype=torch.int32, device=solver.lb.device)
-            # row 0: after the first step (the staged one)
-            A.call("lbm_plan_momentum_exchange", solver._plan, ctypes.c_void_p(links.data_ptr()),
-                   links.shape[0], ctypes.c_void_p(series.data_ptr()), stream_handle())
-            mon = (links, series, count)
+        if not monitor_steps:
+            return None
+        links = solver.solid_links()
+        series = torch.zeros((int(monitor_steps), 2), dtype=torch.float64, device=solver.lb.device)
+        count = torch.ones(1, dtype=torch.int32, device=solver.lb.device)
+        A.call("lbm_plan_momentum_exchange", solver._plan, ctypes.c_void_p(links.data_ptr()),
+               links.shape[0], ctypes.c_void_p(series.data_ptr()), stream_handle())
+        return (links, series, count)
+
+    def add(self, solver, monitor_steps=0, prepared=None):
+        """Join `solver` (beginning its run if needed); returns its slot.
+        `prepared`: the result of Batch.prepare(solver, monitor_steps)."""
+        mon = prepared if prepared is not None else self.prepare(solver, monitor_steps)
         slot = ctypes.c_int32()
         A.call("lbm_batch_add", self._h, solver._plan, ctypes.byref(slot))
         if mon is not None:

@@ -84,10 +84,27 @@ class BoundarySpec:
         self.vectorized = vectorized
 
 
+_GRIDS = {}
+
+
+def _index_grid(nx, ny, ox, oy):
+    """(I, J) index arrays of the box, cached for the last few shapes."""
+    key = (nx, ny, ox, oy)
+    g = _GRIDS.get(key)
+    if g is None:
+        if len(_GRIDS) >= 4:
+            _GRIDS.pop(next(iter(_GRIDS)))
+        g = np.meshgrid(np.arange(nx) + ox, np.arange(ny) + oy, indexing="ij")
+        for a in g:
+            a.setflags(write=False)
+        _GRIDS[key] = g
+    return g
+
+
 def evaluate_predicate(fn, nx, ny, ox=0, oy=0, vectorized=None):
     """Boolean (nx, ny) array of fn over the index box starting at (ox, oy)."""
     if vectorized is not False:
-        I, J = np.meshgrid(np.arange(nx) + ox, np.arange(ny) + oy, indexing="ij")
+        I, J = _index_grid(nx, ny, ox, oy)
         try:
             r = np.asarray(fn(I, J))
             if r.shape == I.shape:

@@ -1,0 +1,221 @@
+"""Serving: simulations admitted as they arrive, run together, returned as
+they finish.
+
+A Server keeps one Batch.  Each request is a cylinder-channel simulation
+(lattice size, collision model, relaxation time or power-law fluid, step
+count) whose populations, mask-derived plan and boundary groups stay on the
+device from admission to completion.  Admission is against an HBM budget:
+a request waits in FIFO order until the bytes its lattice needs fit beside
+the running ones.  The loop is continuous batching: it advances every
+member by a slice of steps (at most `slice_steps`, never past the member
+that finishes first), retires finished members, and admits the requests
+that arrived meanwhile, so work arriving while others run shares the GPU
+with them.  A request's lattice is built by a builder thread on its own
+stream while the batch runs, and joins the batch at the next slice
+boundary after it is ready.
+
+Each result is the same as running the request alone (FusedSolver.step with
+forces), because a batch computes every member with the single-lattice
+arithmetic (see Batch).  Latency is completion minus arrival, in seconds of
+the server's clock.
+"""
+import collections
+import time
+
+import numpy as np
+import torch
+
+from .batch import Batch
+from .workloads import cylinder_channel
+
+
+class Request:
+    """One simulation: an NX x NY channel with a cylinder of radius NY/10
+    at x = NX/5 (centre height NY/2), parabolic inlet u_max, model
+    "bgk" | "trt" | "mrt", relaxation time tau or a power-law fluid (m, n),
+    `steps` time steps, arriving at `arrival` seconds."""
+
+    def __init__(self, rid, nx, ny, model, tau, steps, arrival=0.0, powerlaw=None, umax=0.04,
+                 storage="fp16s"):
+        self.rid, self.nx, self.ny = rid, int(nx), int(ny)
+        self.model, self.tau, self.steps = model, float(tau), int(steps)
+        self.arrival, self.powerlaw, self.umax, self.storage = float(arrival), powerlaw, umax, storage
+        self.admitted = self.finished = None
+        self.forces = None      # (steps, 2) float64 numpy: drag, lift per step
+        self.fields = None      # optional final fields (keep_fields)
+        self.finite = None
+        self.updated_nodes = None
+
+    @property
+    def nodes(self):
+        return self.nx * self.ny
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+    def build(self, tl, keep_init=False):
+        """The request's lattice and solver (cylinder_channel + FusedSolver)."""
+        r = self.ny / 10.0
+        s = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1.0 / self.tau, 1.0 / self.tau] if self.model == "mrt" else None
+        lb, me, coll, be = cylinder_channel(tl, self.nx, self.ny, r, self.nx / 5.0, self.ny / 2.0 - 0.5, self.tau,
+                                            self.umax, model=self.model, mrt_s=s, keep_init=keep_init,
+                                            name=f"req{self.rid}", powerlaw=self.powerlaw)
+        return tl.FusedSolver(lb, me, coll, be, storage=self.storage)
+
+
+def device_bytes(nx, ny, storage):
+    """Bytes of device memory a request of this size holds while served: the
+    LBField's fp32 populations and fields, the plan's population buffers
+    (fp32 or 16-bit), saved moments, node codes and monitors."""
+    pitch = (nx + 31) // 32 * 32
+    per = (2 * 9 * 4            # LBField f, f2 (fp32)
+           + 12 * 4             # rho, total_rho, vel, force, pressure, ... (fp32 fields)
+           + 9 * 4              # collision state (tau / MRT diag)
+           + 2 * 3 * 4          # plan moments (two parities)
+           + 2 + 1)             # node code, mask
+    if storage != "fp32":
+        per += 2 * 9 * 2        # 16-bit population buffers
+    return per * pitch * ny + (1 << 20)
+
+
+class Server:
+    """builders: host threads that build arriving requests' lattices (each
+    on its own CUDA stream) while the scheduler keeps the GPU busy."""
+
+    def __init__(self, tl, hbm_budget, graphs=True, slice_steps=200, keep_fields=False, builders=1):
+        self.tl = tl
+        self.batch = Batch(graphs=graphs)
+        self.budget = int(hbm_budget)
+        self.used = 0
+        self.slice_steps = int(slice_steps)
+        self.keep_fields = keep_fields
+        self.builders = max(1, int(builders))
+        self.queue = collections.deque()
+        self.active = {}        # slot -> [request, solver, remaining steps, bytes]
+        self.done = []
+        self.lattice_updates = 0
+
+    def submit(self, req):
+        if device_bytes(req.nx, req.ny, req.storage) > self.budget:
+            raise ValueError(f"request {req.rid} needs more than the whole HBM budget")
+        self.queue.append(req)
+
+    def _build(self, req, stream):
+        """Builder thread: lattice, plan, first step and first drag/lift row
+        on `stream`; returns what the scheduler needs to join the batch."""
+        with torch.cuda.stream(stream):
+            solver = req.build(self.tl)
+            mon = Batch.prepare(solver, req.steps)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return solver, mon, ev
+
+    def _join(self, req, built, now):
+        solver, mon, ev = built
+        torch.cuda.current_stream().wait_event(ev)
+        slot = self.batch.add(solver, req.steps, prepared=mon)
+        req.admitted = now
+        req.updated_nodes = int(solver.coll.group.n)  # nodes a step updates (fluid and boundary)
+        self.active[slot] = [req, solver, req.steps - 1, device_bytes(req.nx, req.ny, req.storage)]
+
+    def _retire(self, slot, now_fn):
+        req, solver, _, nbytes = self.active.pop(slot)
+        forces = self.batch.forces(slot).cpu().numpy()
+        self.batch.remove(slot)
+        solver.finish()
+        req.forces = forces
+        req.finite = bool(torch.isfinite(solver.lb._rho).all())
+        if self.keep_fields:
+            req.fields = {"rho": solver.lb.rho.to_numpy(), "vel": solver.lb.vel.to_numpy()}
+        torch.cuda.synchronize()
+        req.finished = now_fn()
+        self.used -= nbytes
+        self.done.append(req)
+
+    def run(self, clock=time.perf_counter):
+        """Serve every submitted request (arrival times relative to the start
+        of run); returns the finished requests in completion order."""
+        import concurrent.futures as cf
+        t0 = clock()
+
+        def now():
+            return clock() - t0
+
+        pending = collections.deque(sorted(self.queue, key=lambda r: r.arrival))
+        self.queue.clear()
+        streams = [torch.cuda.Stream() for _ in range(self.builders)]
+        building = collections.deque()  # (request, future) in admission order
+        with cf.ThreadPoolExecutor(self.builders) as pool:
+            n_started = 0
+            while pending or building or self.active:
+                t = now()
+                # admission: arrived requests whose lattice fits the budget go to a builder
+                while pending and pending[0].arrival <= t and \
+                        self.used + device_bytes(pending[0].nx, pending[0].ny, pending[0].storage) <= self.budget:
+                    req = pending.popleft()
+                    self.used += device_bytes(req.nx, req.ny, req.storage)
+                    building.append((req, pool.submit(self._build, req, streams[n_started % self.builders])))
+                    n_started += 1
+                # built lattices join the batch in admission order
+                while building and building[0][1].done():
+                    req, fut = building.popleft()
+                    self._join(req, fut.result(), now())
+                for slot in [s for s, a in self.active.items() if a[2] <= 0]:
+                    self._retire(slot, now)
+                if not self.active:
+                    if building:
+                        building[0][1].result()
+                    elif pending:
+                        time.sleep(max(0.0, min(pending[0].arrival - now(), 0.001)))
+                    continue
+                k = min(self.slice_steps, min(a[2] for a in self.active.values()))
+                self.batch.run(k)
+                for a in self.active.values():
+                    a[2] -= k
+                    self.lattice_updates += k * a[0].updated_nodes
+                for slot in [s for s, a in self.active.items() if a[2] <= 0]:
+                    self._retire(slot, now)
+        for r in self.done:
+            self.lattice_updates += r.updated_nodes  # the staged first step of each request
+        return self.done
+
+    def close(self):
+        self.batch.close()
+
+
+def request_stream(n, rate, seed=20261203, nx_choices=tuple(range(128, 2049, 32)), steps=(2000, 50000),
+                   re_range=(20.0, 200.0), umax=0.04, powerlaw_fraction=0.2, n_range=(0.5, 1.5),
+                   storage="fp16s"):
+    """Seeded cylinder-channel requests with Poisson arrivals at `rate` per
+    second: NX uniform over nx_choices, NY = NX/4, cylinder radius NY/10,
+    Re ~ U[re_range] through tau = 0.5 + 3 u_max (2r) / Re, steps log-uniform
+    in `steps`, model uniform over BGK/TRT/MRT, a fraction of power-law
+    fluids with n ~ U[n_range] and consistency m giving the same Re,
+    m = u_max^(2-n) (2r)^n / Re."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        nx = int(rng.choice(np.asarray(nx_choices)))
+        ny = nx // 4
+        d = 2.0 * ny / 10.0
+        re = rng.uniform(*re_range)
+        tau = 0.5 + 3.0 * umax * d / re
+        st = int(round(np.exp(rng.uniform(np.log(steps[0]), np.log(steps[1])))))
+        model = ["bgk", "trt", "mrt"][int(rng.integers(3))]
+        pl = None
+        if rng.uniform() < powerlaw_fraction:
+            nn = rng.uniform(*n_range)
+            pl = (umax ** (2.0 - nn) * d ** nn / re, nn)
+        out.append(Request(i, nx, ny, model, tau, st, arrival=t, powerlaw=pl, umax=umax, storage=storage))
+    return out
+
+
+def summarize(done, makespan, lattice_updates):
+    lat = np.array([r.latency for r in done])
+    return {"requests": len(done), "makespan_s": round(makespan, 3),
+            "MLUPS": round(lattice_updates / makespan / 1e6, 1),
+            "p50_s": round(float(np.percentile(lat, 50)), 4), "p99_s": round(float(np.percentile(lat, 99)), 4),
+            "finite": int(sum(1 for r in done if r.finite))}

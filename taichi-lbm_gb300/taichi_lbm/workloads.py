@@ -9,40 +9,39 @@ import numpy as np
 
 
 def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=None, magic=0.25,
-                     name="cylinder", keep_init=True):
+                     name="cylinder", keep_init=True, powerlaw=None):
     """Channel with a cylinder: walls on every lattice edge (bounce-back for
     every missing link), periodic stream carrier, parabolic VelocityEquilibrium
     inlet at i = 0 (direction 3), PressureNEEM outlet rho = 1 at i = NX-1
-    (direction 1) — the reference's cylinder case with out-of-range-free groups."""
+    (direction 1) — the reference's cylinder case with out-of-range-free groups.
+    powerlaw=(m, n) makes the fluid a PowerLawFluid (local relaxation)."""
     lb = tl.LBField(name, nx, ny, 1)
     lb.keep_init_snapshot = keep_init
     be = tl.BoundaryEngine()
     be.Mask_cricle_identify(lb, cx, cy, radius)
     cls = tl.BoundaryClassifier((nx, ny))
     mask = lb.mask.arr
+    fluid_arr = mask == 1
+    # a fluid node is a wall node when one of its links has its source outside
+    # the lattice or in the solid
+    src_ok = np.pad(mask != -1, 1, constant_values=False)
+    missing = np.zeros((nx, ny), bool)
+    for k in range(9):
+        ex, ey = int(lb.c[k, 0]), int(lb.c[k, 1])
+        missing |= ~src_ok[1 - ex:1 - ex + nx, 1 - ey:1 - ey + ny]
+    wall_arr = fluid_arr & missing
 
     def fluid_fn(i, j):
-        return mask[i, j] == 1
-
-    def missing_link(i, j):
-        flag = np.zeros(np.shape(i), bool)
-        for k in range(9):
-            i2, j2 = i - lb.c[k, 0], j - lb.c[k, 1]
-            out = (i2 < 0) | (i2 > nx - 1) | (j2 < 0) | (j2 > ny - 1)
-            solid = np.zeros(np.shape(i), bool)
-            ok = ~out
-            solid[ok] = mask[i2[ok], j2[ok]] == -1
-            flag |= out | solid
-        return flag
+        return fluid_arr[i, j]
 
     def wall_fn(i, j):
-        return (mask[i, j] == 1) & missing_link(i, j)
+        return wall_arr[i, j]
 
     def inlet_fn(i, j):
-        return (mask[i, j] == 1) & (i == 0)
+        return fluid_arr[i, j] & (i == 0)
 
     def outlet_fn(i, j):
-        return (mask[i, j] == 1) & (i == nx - 1)
+        return fluid_arr[i, j] & (i == nx - 1)
 
     def parabola(i, j):
         y = j + 0.5
@@ -67,7 +66,8 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
     lb.neighbor_classify()
     me = tl.MacroscopicEngine(fluid.group)
     nu = (tau - 0.5) / 3.0
-    params = {"group": fluid.group, "fluid_model": tl.NewtonianFluid(nu=nu), "NX": nx, "NY": ny,
+    fluid_model = tl.NewtonianFluid(nu=nu) if powerlaw is None else tl.PowerLawFluid(*powerlaw)
+    params = {"group": fluid.group, "fluid_model": fluid_model, "NX": nx, "NY": ny,
               "num_components": 1, "shearviscosity": [nu], "magic": [magic], "bulkviscosity": [nu]}
     if model == "bgk":
         coll = tl.BGKCollision(params)
