@@ -294,6 +294,16 @@ typedef struct LbmPlanBuffers {
    * the current one.                                                       */
   const int32_t* plain;
   int32_t nplain;
+  /* LBM_PIPE_DIRECT with a special list, optional: lane-granular special
+   * work.  lane_mask[y * nseg + seg] has bit l set when one of lane l's
+   * nodes_per_thread nodes is not plain (bounce-back link, boundary program,
+   * saved moments or outside the collision group); lanes lists those lanes
+   * as (y * nseg + seg) * 32 + l, ascending.  A step then runs the plain-path
+   * kernel on every segment, storing only unmarked lanes, and one thread per
+   * listed lane for the rest.                                              */
+  const uint32_t* lane_mask;
+  const int32_t* lanes;
+  int32_t nlanes;
 } LbmPlanBuffers;
 
 typedef struct LbmPlan LbmPlan;
@@ -369,10 +379,17 @@ int lbm_plan_reduce_moments_noalloc(LbmPlan* plan, double* out, void* stream);
  * caller's stream by an event and joined back to it the same way.  With
  * graphs on, two steps are captured once per membership and replayed.
  * Adding, removing or re-monitoring a member rebuilds the tables at the next
- * run; removal waits for the batch's launched work.                        */
+ * run, in stream order (double-buffered tables), without waiting.  The
+ * groups of a step run concurrently on the batch's worker streams.         */
 typedef struct LbmBatch LbmBatch;
 int lbm_batch_create(LbmBatch** out);
-int lbm_batch_add(LbmBatch* batch, LbmPlan* plan, int32_t* slot);
+/* host_lane_mask: a host copy of the plan's lane_mask ([ny][nseg]), or NULL
+ * to read it from the device (a synchronous copy).  Plans other than
+ * Shan-Chen ones must be bound with lane masks. */
+int lbm_batch_add(LbmBatch* batch, LbmPlan* plan, const uint32_t* host_lane_mask, int32_t* slot);
+/* Never waits for the GPU: steps already queued keep reading the member
+ * through the previous tables, so its buffers must outlive them (wait for
+ * the caller's stream before freeing them). */
 int lbm_batch_remove(LbmBatch* batch, int32_t slot);
 /* After every step, append the member's momentum-exchange force (Fx, Fy) on
  * its solid links (site, k pairs, as lbm_plan_momentum_exchange) to

@@ -1,14 +1,18 @@
 // Batch of independent lattices advanced together (C ABI: lbm_batch_*).
 //
 // A batch holds bound plans ("members").  On the first run after a change of
-// membership it groups the members by kernel kind (Shan-Chen tile, plain
+// membership it groups the members by kernel kind (Shan-Chen strip, plain
 // segment, flagged segment) x collision model x power law x storage x nodes
 // per lane x body force, writes one device record per member (its parameters
 // for both ping-pong parities) and one packed tile table, and from then on a
 // step is one persistent launch per group, followed by the drag/lift monitors.
-// The batch runs on its own stream, forked from and joined back to the
-// caller's stream; with graphs enabled it captures two steps (parities 0 and
-// 1) once per membership and replays them.
+// The groups of a step run concurrently on a few worker streams (parallel
+// branches of the graph when graphs are on).  The batch runs on its own
+// stream, forked from and joined back to the caller's stream; with graphs on
+// it captures two steps (parities 0 and 1) once per membership and replays
+// them.  Membership changes never wait for the GPU: the tables are double
+// buffered and written in stream order, so a rebuild is queued behind the
+// steps that still read the previous tables.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -30,6 +34,7 @@ using lbm::BatchTile;
 
 struct BatchMember {
   LbmPlan* plan = nullptr;
+  std::vector<uint32_t> masks;  // host copy of the plan's lane masks
   bool monitored = false;
   const int32_t* links = nullptr;
   int64_t nlinks = 0;
@@ -45,14 +50,25 @@ struct LbmBatch {
   int dev = -1;
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
-  // device tables
-  BatchLattice* d_lats = nullptr;
-  size_t lats_cap = 0;
+  // device tables, double buffered: set `cur` is the one launches read
+  struct Tables {
+    BatchLattice* lats = nullptr;
+    size_t lats_cap = 0;
+    BatchTile* tiles = nullptr;
+    size_t tiles_cap = 0;
+    BatchMonitor* mons = nullptr;
+    size_t mons_cap = 0;
+  } tab[2];
+  int cur = 0;
+  BatchLattice* d_lats = nullptr;  // tab[cur]
   BatchTile* d_tiles = nullptr;
-  size_t tiles_cap = 0;
   BatchMonitor* d_mons = nullptr;
-  size_t mons_cap = 0;
   std::vector<BatchGroup> groups;
+  // worker streams for the groups of one step
+  static constexpr int NWORK = 4;
+  cudaStream_t work[NWORK] = {};
+  cudaEvent_t step_fork = nullptr;
+  cudaEvent_t step_join[NWORK] = {};
   int mon_off[3] = {0, 0, 0}, mon_cnt[3] = {0, 0, 0};  // monitors per storage
   long long ntiles = 0;
   int nlats = 0;
@@ -84,12 +100,31 @@ int launch_monitors(LbmBatch* b, int sp, cudaStream_t s) {
   return LBM_OK;
 }
 
-// one batched step at parity sp on stream s
+// one batched step at parity sp on stream s: the groups on the worker
+// streams (forked from s and joined back), then the monitors on s
 int batch_step(LbmBatch* b, int sp, cudaStream_t s) {
-  for (BatchGroup& g : b->groups) {
-    int rc = launch_group(g, b->d_lats, b->d_tiles, sp, s);
-    if (rc) return rc;
+  const int ng = (int)b->groups.size();
+  if (ng <= 1) {
+    for (BatchGroup& g : b->groups) {
+      int rc = launch_group(g, b->d_lats, b->d_tiles, sp, s);
+      if (rc) return rc;
+    }
+    return launch_monitors(b, sp, s);
   }
+  const int nw = ng < LbmBatch::NWORK ? ng : LbmBatch::NWORK;
+  int rc = lbm_err::cuda(cudaEventRecord(b->step_fork, s), "batch: step fork");
+  for (int w = 0; !rc && w < nw; ++w) rc = lbm_err::cuda(cudaStreamWaitEvent(b->work[w], b->step_fork, 0), "batch: step fork");
+  if (rc) return rc;
+  int rl = LBM_OK;
+  for (int i = 0; i < ng && !rl; ++i) rl = launch_group(b->groups[i], b->d_lats, b->d_tiles, sp, b->work[i % nw]);
+  // join every worker even after a failed launch
+  for (int w = 0; w < nw; ++w) {
+    int rj = lbm_err::cuda(cudaEventRecord(b->step_join[w], b->work[w]), "batch: step join");
+    if (!rj) rj = lbm_err::cuda(cudaStreamWaitEvent(s, b->step_join[w], 0), "batch: step join");
+    if (!rc) rc = rj;
+  }
+  if (rl) return rl;
+  if (rc) return rc;
   return launch_monitors(b, sp, s);
 }
 
@@ -99,14 +134,15 @@ void drop_graph(LbmBatch* b) {
   b->graph_ok = false;
 }
 
+// stream-ordered (re)allocation: launches queued before on s keep their memory
 template <typename T>
-int ensure_capacity(T** ptr, size_t* cap, size_t n, const char* what) {
+int ensure_capacity(T** ptr, size_t* cap, size_t n, cudaStream_t s, const char* what) {
   if (n <= *cap && *ptr) return LBM_OK;
-  if (*ptr) cudaFree(*ptr);
+  if (*ptr) cudaFreeAsync(*ptr, s);
   *ptr = nullptr;
   *cap = 0;
-  const size_t want = std::max<size_t>(n, 1);
-  int rc = lbm_err::cuda(cudaMalloc(reinterpret_cast<void**>(ptr), want * sizeof(T)), what);
+  const size_t want = std::max<size_t>(2 * n, 16);
+  int rc = lbm_err::cuda(cudaMallocAsync(reinterpret_cast<void**>(ptr), want * sizeof(T), s), what);
   if (rc) return rc;
   *cap = want;
   return LBM_OK;
@@ -121,6 +157,11 @@ int ensure_stream(LbmBatch* b) {
   rc = lbm_err::cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "batch: stream");
   if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch: event");
   if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "batch: event");
+  if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->step_fork, cudaEventDisableTiming), "batch: event");
+  for (int w = 0; !rc && w < LbmBatch::NWORK; ++w) {
+    rc = lbm_err::cuda(cudaStreamCreateWithFlags(&b->work[w], cudaStreamNonBlocking), "batch: worker stream");
+    if (!rc) rc = lbm_err::cuda(cudaEventCreateWithFlags(&b->step_join[w], cudaEventDisableTiming), "batch: event");
+  }
   if (rc) return rc;
   b->dev = dev;
   return LBM_OK;
@@ -140,16 +181,16 @@ struct GroupKey {
 
 // rebuild the device records and tile tables from the current members
 int rebuild(LbmBatch* b) {
-  // the previous tables may still be read by launched work
-  int rc = lbm_err::cuda(cudaStreamSynchronize(b->stream), "batch: synchronize before rebuild");
-  if (rc) return rc;
+  // the new tables go to the other buffer set, written in stream order after
+  // the queued steps that still read the current set; a graph being replayed
+  // is freed by the driver when its launches complete
+  int rc = LBM_OK;
   drop_graph(b);
   const int sp = (int)(b->step & 1);
   std::vector<BatchLattice> lats;
   std::map<GroupKey, std::vector<BatchTile>> by_key;  // references stay valid as keys are added
   auto bucket = [&](const GroupKey& k) -> std::vector<BatchTile>& { return by_key[k]; };
   std::vector<BatchMonitor> mons[3];
-  std::vector<uint8_t> flags;
   // rows per Shan-Chen strip: the longest that still gives the GPU enough
   // strips in total (two per resident warp of 152 SMs x 12 warps)
   int sc_rows = 2 * lbm::SC_CHUNK;
@@ -172,6 +213,9 @@ int rebuild(LbmBatch* b) {
       rec.full[v] = lbm_plan_params(pl);
       rec.full[v].special = nullptr;  // the batch supplies its own tiles
       rec.full[v].plain = nullptr;
+      rec.full[v].lane_mask = pl->b.lane_mask;
+      rec.full[v].lanes = nullptr;
+      rec.full[v].nlanes = 0;
       rec.lean[v] = lbm::lean_of(rec.full[v]);
       rec.lean[v].sc_rows = sc_rows;
     }
@@ -185,13 +229,16 @@ int rebuild(LbmBatch* b) {
       const int chunks = (p.ny + sc_rows - 1) / sc_rows;
       for (int item = 0; item < chunks * p.nseg; ++item) t.push_back({lat, item});
     } else {
-      flags.resize((size_t)p.ny * p.nseg);
-      rc = lbm_err::cuda(cudaMemcpy(flags.data(), pl->b.seg_flags, flags.size(), cudaMemcpyDeviceToHost),
-                         "batch: segment flags");
-      if (rc) return rc;
+      // every segment on the plain path (fully marked ones skipped), marked lanes one by one
+      const std::vector<uint32_t>& masks = m.masks;
       auto& tl = bucket({lbm::BATCH_LEAN, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, p.has_force});
       auto& ts = bucket({lbm::BATCH_SPECIAL, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, 0});
-      for (int item = 0; item < (int)flags.size(); ++item) (flags[item] ? ts : tl).push_back({lat, item});
+      for (int item = 0; item < (int)masks.size(); ++item) {
+        const uint32_t mk = masks[item];
+        if (mk != 0xffffffffu) tl.push_back({lat, item});
+        for (int l = 0; l < 32; ++l)
+          if (mk >> l & 1u) ts.push_back({lat, item * 32 + l});
+      }
     }
     if (m.monitored) {
       BatchMonitor bm;
@@ -231,20 +278,28 @@ int rebuild(LbmBatch* b) {
     b->mon_cnt[st] = (int)mons[st].size();
     allm.insert(allm.end(), mons[st].begin(), mons[st].end());
   }
-  rc = ensure_capacity(&b->d_lats, &b->lats_cap, lats.size(), "batch: lattice records");
-  if (!rc) rc = ensure_capacity(&b->d_tiles, &b->tiles_cap, tiles.size(), "batch: tile table");
-  if (!rc) rc = ensure_capacity(&b->d_mons, &b->mons_cap, allm.size(), "batch: monitors");
+  const int nt = b->cur ^ 1;
+  LbmBatch::Tables& T = b->tab[nt];
+  cudaStream_t s = b->stream;
+  rc = ensure_capacity(&T.lats, &T.lats_cap, lats.size(), s, "batch: lattice records");
+  if (!rc) rc = ensure_capacity(&T.tiles, &T.tiles_cap, tiles.size(), s, "batch: tile table");
+  if (!rc) rc = ensure_capacity(&T.mons, &T.mons_cap, allm.size(), s, "batch: monitors");
   if (rc) return rc;
+  // pageable sources: each call returns once its data is staged
   if (!lats.empty())
-    rc = lbm_err::cuda(cudaMemcpy(b->d_lats, lats.data(), lats.size() * sizeof(BatchLattice), cudaMemcpyHostToDevice),
+    rc = lbm_err::cuda(cudaMemcpyAsync(T.lats, lats.data(), lats.size() * sizeof(BatchLattice), cudaMemcpyHostToDevice, s),
                        "batch: upload records");
   if (!rc && !tiles.empty())
-    rc = lbm_err::cuda(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice),
+    rc = lbm_err::cuda(cudaMemcpyAsync(T.tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s),
                        "batch: upload tiles");
   if (!rc && !allm.empty())
-    rc = lbm_err::cuda(cudaMemcpy(b->d_mons, allm.data(), allm.size() * sizeof(BatchMonitor), cudaMemcpyHostToDevice),
+    rc = lbm_err::cuda(cudaMemcpyAsync(T.mons, allm.data(), allm.size() * sizeof(BatchMonitor), cudaMemcpyHostToDevice, s),
                        "batch: upload monitors");
   if (rc) return rc;
+  b->cur = nt;
+  b->d_lats = T.lats;
+  b->d_tiles = T.tiles;
+  b->d_mons = T.mons;
   b->ntiles = (long long)tiles.size();
   b->nlats = (int)lats.size();
   b->dirty = false;
@@ -324,8 +379,10 @@ int lbm_batch_create(LbmBatch** out) {
   return *out ? LBM_OK : lbm_err::set(LBM_ERR_ARG, "batch_create: out of host memory");
 }
 
-int lbm_batch_add(LbmBatch* b, LbmPlan* plan, int32_t* slot) {
+int lbm_batch_add(LbmBatch* b, LbmPlan* plan, const uint32_t* host_lane_mask, int32_t* slot) {
   if (!b || !plan || !slot) return lbm_err::set(LBM_ERR_ARG, "batch_add: NULL argument");
+  if (!plan->d.sc && !plan->b.lane_mask)
+    return lbm_err::set(LBM_ERR_ARG, "batch_add: the plan was bound without lane masks");
   if (!plan->bound) return lbm_err::set(LBM_ERR_STATE, "batch_add: plan not bound");
   const LbmPlanDesc& d = plan->d;
   const int V = d.nodes_per_thread;
@@ -338,8 +395,20 @@ int lbm_batch_add(LbmBatch* b, LbmPlan* plan, int32_t* slot) {
   size_t i = 0;
   while (i < b->slots.size() && b->slots[i].plan) ++i;
   if (i == b->slots.size()) b->slots.emplace_back();
-  b->slots[i] = BatchMember();
-  b->slots[i].plan = plan;
+  BatchMember m;
+  m.plan = plan;
+  if (!d.sc) {
+    m.masks.resize((size_t)d.ny * plan->base.nseg);
+    const size_t bytes = m.masks.size() * sizeof(uint32_t);
+    if (host_lane_mask) {
+      std::memcpy(m.masks.data(), host_lane_mask, bytes);
+    } else {
+      int rc = lbm_err::cuda(cudaMemcpy(m.masks.data(), plan->b.lane_mask, bytes, cudaMemcpyDeviceToHost),
+                             "batch_add: lane masks");
+      if (rc) return rc;
+    }
+  }
+  b->slots[i] = std::move(m);
   b->dirty = true;
   *slot = (int32_t)i;
   return LBM_OK;
@@ -365,11 +434,6 @@ int lbm_batch_monitor(LbmBatch* b, int32_t slot, const int32_t* links, int64_t n
 int lbm_batch_remove(LbmBatch* b, int32_t slot) {
   if (!b || slot < 0 || slot >= (int32_t)b->slots.size() || !b->slots[slot].plan)
     return lbm_err::set(LBM_ERR_ARG, "batch_remove: no member in slot %d", slot);
-  // launched work may still read the member's buffers through the tables
-  if (b->stream) {
-    int rc = lbm_err::cuda(cudaStreamSynchronize(b->stream), "batch_remove: synchronize");
-    if (rc) return rc;
-  }
   b->slots[slot] = BatchMember();
   b->dirty = true;
   return LBM_OK;
@@ -414,9 +478,16 @@ int lbm_batch_destroy(LbmBatch* b) {
   if (!b) return LBM_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  if (b->d_lats) cudaFree(b->d_lats);
-  if (b->d_tiles) cudaFree(b->d_tiles);
-  if (b->d_mons) cudaFree(b->d_mons);
+  for (LbmBatch::Tables& t : b->tab) {
+    if (t.lats) cudaFree(t.lats);
+    if (t.tiles) cudaFree(t.tiles);
+    if (t.mons) cudaFree(t.mons);
+  }
+  for (int w = 0; w < LbmBatch::NWORK; ++w) {
+    if (b->work[w]) cudaStreamDestroy(b->work[w]);
+    if (b->step_join[w]) cudaEventDestroy(b->step_join[w]);
+  }
+  if (b->step_fork) cudaEventDestroy(b->step_fork);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
   if (b->stream) cudaStreamDestroy(b->stream);

@@ -4,7 +4,8 @@
 // Every lattice has a device record with two views of its parameters (the
 // populations and saved moments read from / written to, for the two
 // ping-pong parities).  A tile is (lattice, item): for the plain and flagged
-// kinds an item is one row segment (y * nseg + seg), for Shan-Chen one
+// kind an item is one row segment (y * nseg + seg), for the marked-lane kind
+// one lane ((y * nseg + seg) * 32 + lane), for Shan-Chen one
 // strip of 32V columns and SC_CHUNK rows (chunk * nseg + seg).  The kernels
 // are persistent: a grid sized to the GPU walks the table, a warp per tile,
 // and copies a lattice's parameters into the warp's shared memory when its
@@ -52,38 +53,29 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLatt
     const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
     const int seg = tile.item - y * p.nseg;
     const int x0s = seg * 32 * V, x0 = x0s + lane * V;
+    uint32_t mask;  // lanes k_batch_lanes stores
+    ldg_early(p.lane_mask + tile.item, mask);
     float h[V][9];
     if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
     else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
-    lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+    if (mask == 0xffffffffu) continue;
+    lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0, (mask >> lane) & 1u);
   }
 }
 
-// Flagged segments (bounce-back links, boundary programs, saved moments,
-// inactive nodes) of every lattice in the table: the general path.
+// Marked lanes (bounce-back links, boundary programs, saved moments,
+// inactive nodes) of every lattice in the table, one thread per lane entry
+// ((y * nseg + seg) * 32 + lane): the general per-node path.
 template <int MODEL, bool PL, int ST, int V>
-__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_special(const BatchLattice* __restrict__ lats,
-                                                                     const BatchTile* __restrict__ tiles,
-                                                                     int ntiles, int sp) {
-  __shared__ FusedParams fp[BATCH_WARPS];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  FusedParams& p = fp[warp];
-  int cur = -1;
-  for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
-    const BatchTile tile = tiles[t];
-    if (tile.lat != cur) {
-      __syncwarp();
-      copy_words(&p, &lats[tile.lat].full[view_of(lats, tile.lat, sp)], lane, 32);
-      __syncwarp();
-      cur = tile.lat;
-    }
-    const int y = tile.item / p.nseg;
-    const int seg = tile.item - y * p.nseg;
-    const int x0 = seg * 32 * V + lane * V;
-    float f[V][9];
-    gather_direct<ST, V>(p, y, seg, lane, f);
-    fused_tail<MODEL, PL, ST, V>(p, f, y, seg, x0, x0 < p.nx);
-  }
+__global__ void __launch_bounds__(128) k_batch_lanes(const BatchLattice* __restrict__ lats,
+                                                     const BatchTile* __restrict__ tiles, int ntiles, int sp) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const BatchTile tile = tiles[t];
+  const FusedParams& p = lats[tile.lat].full[view_of(lats, tile.lat, sp)];
+  const int item = tile.item >> 5, lane = tile.item & 31;
+  const int y = item / p.nseg;
+  lane_general<MODEL, PL, ST, V>(p, y, (item - y * p.nseg) * 32 * V + lane * V);
 }
 
 // Shan-Chen strips (item = chunk * nseg + seg) of every lattice in the
@@ -194,11 +186,8 @@ int launch_batch_seg(BatchGroup& g, const BatchLattice* lats, const BatchTile* t
   if (g.count == 0) return LBM_OK;
   const BatchTile* t = tiles + g.offset;
   if (g.kind == BATCH_SPECIAL) {
-    auto kern = k_batch_special<MODEL, PL, ST, V>;
-    const int b = batch_grid(kern, BATCH_WARPS * 32, BATCH_WARPS, g.count, &g.blocks);
-    if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
-    kern<<<b, BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
-    return lbm_err::launch("batched step (flagged segments)");
+    k_batch_lanes<MODEL, PL, ST, V><<<(unsigned)((g.count + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
+    return lbm_err::launch("batched step (marked lanes)");
   }
   auto kern = g.force ? k_batch_lean<MODEL, PL, ST, V, 1> : k_batch_lean<MODEL, PL, ST, V, 0>;
   const int b = batch_grid(kern, BATCH_WARPS * 32, BATCH_WARPS, g.count, &g.blocks);

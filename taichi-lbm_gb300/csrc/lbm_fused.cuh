@@ -55,6 +55,12 @@ struct FusedParams {
   const int32_t* plain;
   int nplain;
   int tune;  // LBM_PIPE_ASYNC / LBM_PIPE_PREFETCH tuning index
+  // lane-granular two-pass step: bit l of lane_mask[y * nseg + seg] marks a
+  // lane with a node that is not plain; lanes lists those lanes
+  // ((y * nseg + seg) * 32 + lane), handled by k_fused_lanes
+  const uint32_t* lane_mask;
+  const int32_t* lanes;
+  int nlanes;
   // 16-bit storage holds f_k - wsh[k], wsh[k] = w_k * rho_ref (the plan's
   // reference density); fp32 storage ignores it
   float wsh[9];
@@ -82,6 +88,7 @@ struct LeanParams {
   float g_coh, sc_T;
   LbmEos eos;
   int sc_rows;  // rows of a strip item
+  const uint32_t* lane_mask;  // lanes not to store (FusedParams::lane_mask), or null
 };
 
 // Division by an invariant divisor d (1 <= d < 2^31) as a multiply-high and
@@ -129,6 +136,7 @@ inline LeanParams lean_of(const FusedParams& f) {
   l.sc_T = f.sc_T;
   l.eos = f.eos;
   l.sc_rows = 16;
+  l.lane_mask = f.lane_mask;
   return l;
 }
 
@@ -576,6 +584,63 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
     for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], p.wsh[k]);
     store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
   }
+}
+
+// The general step of one lane's V nodes (x0.., row y) from per-node
+// gathers: what fused_tail does for a whole segment, for a lane the lane
+// mask marks.  A node outside the collision group keeps its stored values
+// (copied bit for bit).
+template <int MODEL, bool PL, int ST, int V>
+__device__ __forceinline__ void lane_general(const FusedParams& p, int y, int x0) {
+  using S = Storage<ST>;
+  using T = typename S::T;
+  const T* src = reinterpret_cast<const T*>(p.src);
+  T* dst = reinterpret_cast<T*>(p.dst);
+  const float Fx = p.has_force ? p.gx : 0.0f, Fy = p.has_force ? p.gy : 0.0f;
+#pragma unroll 1
+  for (int i = 0; i < V; ++i) {
+    const int x = x0 + i;
+    if (x >= p.nx) break;
+    const size_t q = (size_t)y * p.pitch + x;
+    const unsigned code = p.code[q];
+    if (!(code & LBM_CODE_ACTIVE)) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = load1(src + (size_t)k * p.plane + q);
+      continue;
+    }
+    float f[9];
+    gather_node<ST>(p, x, y, f);
+    const unsigned prog = code >> LBM_CODE_PROG_SHIFT;
+    for (int s = 0; prog && s < LBM_PROG_LEN; ++s) {
+      const int bi = p.prog[prog][s];
+      if (bi < 0) break;
+      apply_bc<ST>(p, bi, x, y, f);
+    }
+    const float rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const float jx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
+    const float jy = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
+    const float ux = (jx + 0.5f * Fx) / rho, uy = (jy + 0.5f * Fy) / rho;
+    if (code & LBM_CODE_SAVE) {
+      p.mom_out[q] = rho;
+      p.mom_out[p.plane + q] = ux;
+      p.mom_out[2 * p.plane + q] = uy;
+    }
+    const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
+    if (PL) p.tau[q] = st;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k]);
+  }
+}
+
+// One thread per listed lane.
+template <int MODEL, bool PL, int ST, int V>
+__global__ void __launch_bounds__(128) k_fused_lanes(const FusedParams p) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.nlanes) return;
+  const int e = p.lanes[t];
+  const int item = e >> 5, lane = e & 31;
+  const int y = item / p.nseg;
+  lane_general<MODEL, PL, ST, V>(p, y, (item - y * p.nseg) * 32 * V + lane * V);
 }
 
 // Stream + boundary pass only (the last half step of a fused run): writes the

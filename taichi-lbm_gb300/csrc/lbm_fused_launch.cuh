@@ -148,7 +148,13 @@ int launch_pf_tuned(const FusedParams& p, cudaStream_t s) {
 // passing another stream has forked it from s and joins it back after.
 template <int MODEL, bool PL, int ST, int V>
 int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s, cudaStream_t s2) {
-  if (p.nspecial > 0) {
+  if (p.lane_mask) {  // lane-granular form: the marked lanes, then every segment
+    if (p.nlanes > 0) {
+      k_fused_lanes<MODEL, PL, ST, V><<<(unsigned)((p.nlanes + 127) / 128), 128, 0, s2>>>(p);
+      int rc = lbm_err::launch("fused step (marked lanes)");
+      if (rc) return rc;
+    }
+  } else if (p.nspecial > 0) {
     k_fused_special<MODEL, PL, ST, V><<<(unsigned)((p.nspecial + 7) / 8), 256, 0, s2>>>(p);
     int rc = lbm_err::launch("fused step (flagged segments)");
     if (rc) return rc;

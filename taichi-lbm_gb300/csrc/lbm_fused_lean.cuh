@@ -431,9 +431,9 @@ __device__ __forceinline__ float collide_lean(const P& p, float h[9], float stat
 // Moments, collision and stores of one lane's V nodes (x0.., row y) of a
 // plain segment, from the gathered stored values h.
 template <class P, int MODEL, bool PL, int ST, int V, int FORCE>
-__device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9], int y, int x0) {
+__device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9], int y, int x0, bool skip = false) {
   using T = typename Storage<ST>::T;
-  const bool live = x0 < p.nx;
+  const bool live = x0 < p.nx && !skip;  // skip: another kernel stores this lane
   const size_t rowoff = (size_t)y * p.pitch;
   float tau[V];
   if (PL) {
@@ -476,14 +476,22 @@ __global__ void __launch_bounds__(256) k_fused_bulk(const FusedParams p) {
   const int y = blockIdx.y + gridDim.y * blockIdx.z;
   const int seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (seg >= p.nseg || y >= p.ny) return;
-  unsigned char flag;
-  ldg_early(p.seg_flags + (size_t)y * p.nseg + seg, flag);
+  // with lane masks every segment is gathered here and the marked lanes are
+  // stored by k_fused_lanes; else k_fused_special owns a flagged segment
+  uint32_t mask;
+  if (p.lane_mask) {
+    ldg_early(p.lane_mask + (size_t)y * p.nseg + seg, mask);
+  } else {
+    unsigned char flag;
+    ldg_early(p.seg_flags + (size_t)y * p.nseg + seg, flag);
+    mask = flag ? 0xffffffffu : 0u;
+  }
   const int x0s = seg * 32 * V, x0 = x0s + lane * V;
   float h[V][9];
   if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<FusedParams, ST, V>(p, y, x0, lane, h);
   else gather_edge<FusedParams, ST, V>(p, y, x0, lane, h);
-  if (flag) return;  // uniform over the warp: k_fused_special owns this segment
-  lean_collide_store<FusedParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0);
+  if (mask == 0xffffffffu) return;  // uniform over the warp
+  lean_collide_store<FusedParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0, (mask >> lane) & 1u);
 }
 
 // ------------------------------------------------------------ prefetching form

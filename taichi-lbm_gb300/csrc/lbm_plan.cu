@@ -35,6 +35,12 @@ FusedParams params_for(const LbmPlan* pl) {
   p.nspecial = two ? pl->b.nspecial : 0;
   p.plain = two && pl->d.pipeline == LBM_PIPE_PREFETCH ? pl->b.plain : nullptr;
   p.nplain = p.plain ? pl->b.nplain : 0;
+  // lane-granular special work (direct pipeline): every segment on the lean
+  // kernel, the marked lanes on k_fused_lanes
+  const bool lanes = two && pl->d.pipeline == LBM_PIPE_DIRECT && pl->b.lane_mask && pl->b.lanes;
+  p.lane_mask = lanes ? pl->b.lane_mask : nullptr;
+  p.lanes = lanes ? pl->b.lanes : nullptr;
+  p.nlanes = lanes ? pl->b.nlanes : 0;
   return p;
 }
 
@@ -94,7 +100,7 @@ int ensure_side(LbmPlan* pl) {
 // one fused step on stream s and the parity flip
 int step_once(LbmPlan* pl, cudaStream_t s) {
   FusedParams p = params_for(pl);
-  const bool fork = p.special && p.nspecial > 0 && pl->b.special_stream;
+  const bool fork = p.special && (p.lane_mask ? p.nlanes > 0 : p.nspecial > 0) && pl->b.special_stream;
   cudaStream_t s2 = s;
   if (fork) {
     int rc = ensure_side(pl);
@@ -230,6 +236,10 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
       (int64_t)b->nspecial > (int64_t)pl->d.ny * pl->base.nseg)
     return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d special segments for a %d x %d segment grid", b->nspecial,
                         pl->d.ny, pl->base.nseg);
+  if (b->nlanes < 0 || (b->nlanes > 0 && !b->lanes) || (b->lanes && !b->lane_mask) ||
+      (int64_t)b->nlanes > (int64_t)pl->d.ny * pl->base.nseg * 32)
+    return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d marked lanes for a %d x %d segment grid", b->nlanes, pl->d.ny,
+                        pl->base.nseg);
   if (b->nplain < 0 || (b->nplain > 0 && !b->plain) ||
       (int64_t)b->nplain + b->nspecial > (int64_t)pl->d.ny * pl->base.nseg)
     return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d plain + %d special segments for a %d x %d segment grid",

@@ -77,7 +77,9 @@ class LbmPlanBuffers(ctypes.Structure):
     _fields_ = [(n, _vp) for n in ("fa", "fb", "mom_a", "mom_b", "code", "seg_flags", "bc_vel",
                                    "tau", "status", "special")] + [("nspecial", ctypes.c_int32),
                                                            ("special_stream", ctypes.c_int32),
-                                                           ("plain", _vp), ("nplain", ctypes.c_int32)]
+                                                           ("plain", _vp), ("nplain", ctypes.c_int32),
+                                                           ("lane_mask", _vp), ("lanes", _vp),
+                                                           ("nlanes", ctypes.c_int32)]
 
 
 class LbmError(RuntimeError):
@@ -128,7 +130,7 @@ _SIGS = {
     "lbm_plan_reduce_moments_noalloc": ([_vp, _vp, _vp], ctypes.c_int),
     "lbm_plan_reduce_moments": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "lbm_batch_create": ([_vp], ctypes.c_int),
-    "lbm_batch_add": ([_vp, _vp, _vp], ctypes.c_int),
+    "lbm_batch_add": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "lbm_batch_remove": ([_vp, ctypes.c_int32], ctypes.c_int),
     "lbm_batch_monitor": ([_vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int32], ctypes.c_int),
     "lbm_batch_set_graph": ([_vp, ctypes.c_int32], ctypes.c_int),

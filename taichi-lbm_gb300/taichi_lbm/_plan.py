@@ -259,8 +259,14 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
     pad = nseg * seg_w - nx
     notplain = np.pad(~plain, ((0, pad), (0, 0)), constant_values=False)
     seg_flags = notplain.reshape(nseg, seg_w, ny).any(axis=1).T.astype(np.uint8)  # (ny, nseg)
+    # lane masks: bit l of (y, seg) is set when one of lane l's V nodes is not plain
+    lane_special = notplain.reshape(nseg, 32, V, ny).any(axis=2).transpose(2, 0, 1)  # (ny, nseg, 32)
+    bits = (np.uint64(1) << np.arange(32, dtype=np.uint64))
+    lane_mask = (lane_special.astype(np.uint64) * bits).sum(axis=2).astype(np.uint32)  # (ny, nseg)
+    lanes = np.flatnonzero(lane_special.ravel()).astype(np.int32)  # (y * nseg + seg) * 32 + lane
 
     return CompiledPlan(code=code.astype(np.uint16), seg_flags=np.ascontiguousarray(seg_flags),
+                        lane_mask=np.ascontiguousarray(lane_mask), lanes=lanes,
                         nseg=nseg, instances=instances, programs=programs, nprog=len(seqs) + 1,
                         bc_vel=bc_vel, items=items, active=active, save=save,
                         n_special_segments=int(seg_flags.sum()))

@@ -14,6 +14,7 @@ float64 CUDA tensor, the series FusedSolver.step(n, forces=True) returns.
 """
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _capi as A
@@ -51,7 +52,11 @@ class Batch:
         `prepared`: the result of Batch.prepare(solver, monitor_steps)."""
         mon = prepared if prepared is not None else self.prepare(solver, monitor_steps)
         slot = ctypes.c_int32()
-        A.call("lbm_batch_add", self._h, solver._plan, ctypes.byref(slot))
+        masks = None
+        if solver.sc is None:
+            masks = np.ascontiguousarray(np.asarray(solver.compiled.lane_mask, np.uint32))
+        A.call("lbm_batch_add", self._h, solver._plan,
+               None if masks is None else masks.ctypes.data_as(ctypes.c_void_p), ctypes.byref(slot))
         if mon is not None:
             links, series, count = mon
             A.call("lbm_batch_monitor", self._h, slot.value, ctypes.c_void_p(links.data_ptr()),
@@ -61,7 +66,9 @@ class Batch:
         return slot.value
 
     def remove(self, slot):
-        """Leave the batch; returns the solver (its state stays live)."""
+        """Leave the batch; returns the solver (its state stays live).  Steps
+        already queued still compute the member: work on the current stream
+        after this call (finish(), reading its fields) follows them."""
         A.call("lbm_batch_remove", self._h, int(slot))
         solver, _ = self.members.pop(int(slot))
         return solver

@@ -119,19 +119,36 @@ class Server:
         req.updated_nodes = int(solver.coll.group.n)  # nodes a step updates (fluid and boundary)
         self.active[slot] = [req, solver, req.steps - 1, device_bytes(req.nx, req.ny, req.storage)]
 
-    def _retire(self, slot, now_fn):
-        req, solver, _, nbytes = self.active.pop(slot)
-        forces = self.batch.forces(slot).cpu().numpy()
-        self.batch.remove(slot)
-        solver.finish()
-        req.forces = forces
-        req.finite = bool(torch.isfinite(solver.lb._rho).all())
-        if self.keep_fields:
-            req.fields = {"rho": solver.lb.rho.to_numpy(), "vel": solver.lb.vel.to_numpy()}
-        torch.cuda.synchronize()
+    def _retire(self, entry, now_fn):
+        """Finish a member that left the batch: on the retire stream, after
+        the event of the slice it finished in (later slices keep running)."""
+        (req, solver, _, nbytes), mon, ev = entry
+        with torch.cuda.stream(self.retire_stream):
+            self.retire_stream.wait_event(ev)
+            _, series, count = mon
+            n = min(int(count.item()), series.shape[0])
+            req.forces = series[:n].cpu().numpy()
+            solver.finish()
+            req.finite = bool(torch.isfinite(solver.lb._rho).all())
+            if self.keep_fields:
+                req.fields = {"rho": solver.lb.rho.to_numpy(), "vel": solver.lb.vel.to_numpy()}
+            self.retire_stream.synchronize()
         req.finished = now_fn()
         self.used -= nbytes
         self.done.append(req)
+
+    def _leave(self, retiring):
+        """Members at zero remaining steps leave the batch (no wait); their
+        retirement is queued behind an event of the current stream."""
+        gone = [s for s, a in self.active.items() if a[2] <= 0]
+        if not gone:
+            return
+        ev = torch.cuda.Event()
+        ev.record()
+        for slot in gone:
+            mon = self.batch.members[slot][1]
+            self.batch.remove(slot)
+            retiring.append((self.active.pop(slot), mon, ev))
 
     def run(self, clock=time.perf_counter):
         """Serve every submitted request (arrival times relative to the start
@@ -145,10 +162,12 @@ class Server:
         pending = collections.deque(sorted(self.queue, key=lambda r: r.arrival))
         self.queue.clear()
         streams = [torch.cuda.Stream() for _ in range(self.builders)]
+        self.retire_stream = torch.cuda.Stream()
         building = collections.deque()  # (request, future) in admission order
+        retiring = []                   # members that left, with the event to wait for
         with cf.ThreadPoolExecutor(self.builders) as pool:
             n_started = 0
-            while pending or building or self.active:
+            while pending or building or self.active or retiring:
                 t = now()
                 # admission: arrived requests whose lattice fits the budget go to a builder
                 while pending and pending[0].arrival <= t and \
@@ -161,21 +180,25 @@ class Server:
                 while building and building[0][1].done():
                     req, fut = building.popleft()
                     self._join(req, fut.result(), now())
-                for slot in [s for s, a in self.active.items() if a[2] <= 0]:
-                    self._retire(slot, now)
-                if not self.active:
-                    if building:
-                        building[0][1].result()
-                    elif pending:
-                        time.sleep(max(0.0, min(pending[0].arrival - now(), 0.001)))
-                    continue
-                k = min(self.slice_steps, min(a[2] for a in self.active.values()))
-                self.batch.run(k)
-                for a in self.active.values():
-                    a[2] -= k
-                    self.lattice_updates += k * a[0].updated_nodes
-                for slot in [s for s, a in self.active.items() if a[2] <= 0]:
-                    self._retire(slot, now)
+                self._leave(retiring)  # single-step requests
+                launched = False
+                if self.active:
+                    k = min(self.slice_steps, min(a[2] for a in self.active.values()))
+                    self.batch.run(k)
+                    launched = True
+                    for a in self.active.values():
+                        a[2] -= k
+                        self.lattice_updates += k * a[0].updated_nodes
+                # retire what finished in earlier slices while this one runs
+                for entry in retiring:
+                    self._retire(entry, now)
+                retiring = []
+                if launched:
+                    self._leave(retiring)
+                elif building:
+                    building[0][1].result()
+                elif pending:
+                    time.sleep(max(0.0, min(pending[0].arrival - now(), 0.001)))
         for r in self.done:
             self.lattice_updates += r.updated_nodes  # the staged first step of each request
         return self.done

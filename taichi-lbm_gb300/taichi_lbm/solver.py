@@ -47,8 +47,9 @@ def boundary_items(boundary_engine):
 class FusedSolver:
     def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
                  nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
-                 sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True):
+                 sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True, lane_special=True):
         self.sc = lb_field.sc_field
+        self.lane_special = bool(lane_special)
         self.two_pass = bool(two_pass)
         self.overlap = bool(overlap)
         self.rho_ref = rho_ref
@@ -202,6 +203,9 @@ class FusedSolver:
         self.nspecial = int(flagged.size)
         self.plain = torch.as_tensor(plain if plain.size else np.zeros(1, np.int32), device=dev)
         self.nplain = int(plain.size)
+        self.lane_mask = torch.as_tensor(cp.lane_mask.view(np.int32), device=dev)
+        self.lanes = torch.as_tensor(cp.lanes if cp.lanes.size else np.zeros(1, np.int32), device=dev)
+        self.nlanes = int(cp.lanes.size)
         self.mom = [torch.zeros((3, ny, P), dtype=torch.float32, device=dev) for _ in range(2)]
         if self.storage == A.STORE_F32:
             self.fbuf = None
@@ -239,6 +243,8 @@ class FusedSolver:
             b.special_stream = 1 if self.overlap else 0
             if self.pipeline == A.PIPE_PREFETCH:
                 b.plain, b.nplain = self.plain.data_ptr(), self.nplain
+            elif self.lane_special:
+                b.lane_mask, b.lanes, b.nlanes = self.lane_mask.data_ptr(), self.lanes.data_ptr(), self.nlanes
         A.call("lbm_plan_bind", self._plan, ctypes.byref(b))
 
     def _moments(self):

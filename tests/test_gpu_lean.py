@@ -133,9 +133,29 @@ def test_prefetch_tunings_match_direct(tl, tune, shape):
     out = []
     for pipeline, t in (("direct", 0), ("prefetch", tune)):
         lb, me, coll, be = cylinder_channel(tl, nx, ny, ny / 10, nx / 5, ny / 2 - 0.5, 0.56, 0.05, model="trt")
-        solver = tl.FusedSolver(lb, me, coll, be, storage="fp16s", pipeline=pipeline, tune=t)
+        # both with per-segment special work (the prefetching form has no lane form)
+        solver = tl.FusedSolver(lb, me, coll, be, storage="fp16s", pipeline=pipeline, tune=t,
+                                lane_special=False)
         assert solver.launches_per_step == 2
         solver.step(60)
         out.append(fields_of(lb))
     for k in ("f", "f2", "rho", "vel"):
         assert rel_err(out[1][k], out[0][k]) == 0.0, k
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("shape", [(520, 64), (200, 48)])
+def test_lane_special_equals_segment_special(tl, storage, shape):
+    """Special work per lane (the plain kernel on every segment, one thread
+    per marked lane) and per segment (the general kernel on every flagged
+    segment) give the same step; 200 columns make most segments flagged."""
+    nx, ny = shape
+    out = []
+    for lane_special in (False, True):
+        lb, me, coll, be = cylinder_channel(tl, nx, ny, ny / 10, nx / 5, ny / 2 - 0.5, 0.56, 0.05, model="trt")
+        solver = tl.FusedSolver(lb, me, coll, be, storage=storage, lane_special=lane_special)
+        solver.step(80)
+        out.append(fields_of(lb))
+    tol = TOL if storage == "fp32" else STORE_TOL[storage]
+    for k in ("rho", "vel"):
+        assert rel_err(out[1][k], out[0][k]) <= tol, k
