@@ -72,10 +72,10 @@ class CompiledPlan:
 
 
 def _members(nx, ny, nodes):
-    m = np.zeros((nx, ny), bool)
+    m = np.zeros(nx * ny, bool)
     if nodes.size:
-        m[nodes[:, 0], nodes[:, 1]] = True
-    return m
+        m[nodes[:, 0].astype(np.int64) * ny + nodes[:, 1]] = True
+    return m.reshape(nx, ny)
 
 
 def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
@@ -83,25 +83,28 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
     has a source; bit 15: node classified)."""
     V = int(nodes_per_thread)
     active = _members(nx, ny, np.asarray(collision_nodes, np.int32).reshape(-1, 2))
-    carrier = np.full((nx, ny), -1, np.int32)
-    carrier_kind = np.zeros((nx, ny), np.int32)
-    covered = np.zeros((nx, ny), bool)
+    carrier = np.full(nx * ny, -1, np.int32)  # flat views, scattered by linear index
+    carrier_kind = np.zeros(nx * ny, np.int32)
+    covered = np.zeros(nx * ny, bool)
     rewrites = []
     for idx, it in enumerate(items):
         nd = it.nodes
-        if nd.size and ((nd[:, 0] < 0).any() or (nd[:, 0] >= nx).any() or (nd[:, 1] < 0).any()
-                        or (nd[:, 1] >= ny).any()):
+        if nd.size and (nd.min(axis=0) < 0).any() | (nd[:, 0].max() >= nx) | (nd[:, 1].max() >= ny):
             raise UnsupportedComposition(f"boundary '{it.name}' has nodes outside the lattice")
         if it.kind == A.BC_FLUID:
             continue
-        covered[nd[:, 0], nd[:, 1]] = True
+        lin = nd[:, 0].astype(np.int64) * ny + nd[:, 1]
+        covered[lin] = True
         if it.kind in (A.BC_PERIODIC, A.BC_INSIDE, A.BC_BOUNCEBACK):
-            carrier[nd[:, 0], nd[:, 1]] = idx
-            carrier_kind[nd[:, 0], nd[:, 1]] = it.kind
+            carrier[lin] = idx
+            carrier_kind[lin] = it.kind
         elif it.kind in READS:
             rewrites.append(idx)
         else:
             raise UnsupportedComposition(f"boundary '{it.name}' (kind {it.kind}) has no fused form")
+    carrier = carrier.reshape(nx, ny)
+    carrier_kind = carrier_kind.reshape(nx, ny)
+    covered = covered.reshape(nx, ny)
 
     if (active & (carrier < 0)).any():
         i, j = np.argwhere(active & (carrier < 0))[0]
@@ -112,7 +115,8 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
         raise UnsupportedComposition(f"node ({i}, {j}) is in a boundary group but not in the "
                                      "collision group")
 
-    # --- bounce bits from each node's last carrier
+    # --- bounce bits from each node's last carrier: bit k-1 of the code is set
+    # when link k has no source (bit k of the neighbor bits clear)
     code = np.zeros((nx, ny), np.int64)
     code[active] |= A.CODE_ACTIVE
     links = np.asarray(links, np.int64)
@@ -122,13 +126,13 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
         i, j = np.argwhere((bb | ins) & ((links & 0x8000) == 0))[0]
         raise UnsupportedComposition(f"node ({i}, {j}) streams through the neighbor table but "
                                      "was never classified (call neighbor_classify after the mask)")
-    for k in range(1, 9):
-        missing = ((links >> k) & 1) == 0
-        if (ins & missing).any():
-            i, j = np.argwhere(ins & missing)[0]
-            raise UnsupportedComposition(f"InsideBoundary node ({i}, {j}) has no source on link "
-                                         f"{k}: the reference reads outside the lattice there")
-        code[bb & missing] |= 1 << (k - 1)
+    missing_bits = (~links >> 1) & 0xFF
+    if (ins & (missing_bits != 0)).any():
+        i, j = np.argwhere(ins & (missing_bits != 0))[0]
+        k = int(np.flatnonzero([(missing_bits[i, j] >> b) & 1 for b in range(8)])[0]) + 1
+        raise UnsupportedComposition(f"InsideBoundary node ({i}, {j}) has no source on link "
+                                     f"{k}: the reference reads outside the lattice there")
+    code |= np.where(bb, missing_bits, 0)
 
     # --- rewrite boundaries: ordering checks, reads, saves
     member = {idx: _members(nx, ny, items[idx].nodes) for idx in rewrites}
@@ -220,31 +224,43 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
         bc_vel[1, nd[:, 0], nd[:, 1]] = v[:, 1]
         vel_owner[nd[:, 0], nd[:, 1]] = idx
 
-    # programs: ordered instance list per node
+    # programs: ordered instance list per node, as a base-(MAX_BC + 1) key
+    # (a boundary merged into the previous instance adds nothing)
     seqs = {}
     node_prog = np.zeros((nx, ny), np.int64)
     if rewrites:
-        lists = {}
+        base = A.MAX_BC + 1
+        key = np.zeros(nx * ny, np.int64)
+        length = np.zeros(nx * ny, np.int32)
+        last = np.full(nx * ny, -1, np.int32)
         for idx in rewrites:
-            nd = items[idx].nodes
             n = inst_of_item.get(idx)
-            if n is None:
+            nd = items[idx].nodes
+            if n is None or nd.size == 0:
                 continue
-            for i, j in nd:
-                lst = lists.setdefault((int(i), int(j)), [])
-                if not lst or lst[-1] != n:
-                    lst.append(n)
-        for (i, j), lst in lists.items():
-            t = tuple(lst)
-            if len(t) > A.PROG_LEN:
-                raise UnsupportedComposition(f"node ({i}, {j}) has {len(t)} rewrite boundaries "
-                                             f"(at most {A.PROG_LEN})")
-            if t not in seqs:
-                seqs[t] = len(seqs) + 1
-            node_prog[i, j] = seqs[t]
-        if len(seqs) + 1 > A.MAX_PROG:
-            raise UnsupportedComposition(f"{len(seqs)} distinct boundary programs "
+            lin = nd[:, 0].astype(np.int64) * ny + nd[:, 1]
+            lin = lin[last[lin] != n]
+            key[lin] = key[lin] * base + (n + 1)
+            length[lin] += 1
+            last[lin] = n
+        if (length > A.PROG_LEN).any():
+            q = int(np.flatnonzero(length > A.PROG_LEN)[0])
+            raise UnsupportedComposition(f"node ({q // ny}, {q % ny}) has {int(length[q])} rewrite "
+                                         f"boundaries (at most {A.PROG_LEN})")
+        has = length > 0
+        keys, inv = np.unique(key[has], return_inverse=True)
+        if keys.size + 1 > A.MAX_PROG:
+            raise UnsupportedComposition(f"{keys.size} distinct boundary programs "
                                          f"(at most {A.MAX_PROG - 1})")
+        for pid, kv in enumerate(keys.tolist(), start=1):
+            digits = []
+            while kv:
+                digits.append(kv % base - 1)
+                kv //= base
+            seqs[tuple(reversed(digits))] = pid
+        flat = np.zeros(nx * ny, np.int64)
+        flat[has] = inv + 1
+        node_prog = flat.reshape(nx, ny)
     code |= node_prog << A.CODE_PROG_SHIFT
     code[save & active] |= A.CODE_SAVE
 

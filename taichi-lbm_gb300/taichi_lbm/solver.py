@@ -370,22 +370,18 @@ class FusedSolver:
             return self._solid_links
         lb = self.lb
         code = self.compiled.code.astype(np.int64)
-        mask = lb.mask.arr
         nx, ny = lb.NX, lb.NY
-        I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
-        cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
-        cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
-        opp = [0, 3, 4, 1, 2, 7, 8, 5, 6]
+        solid = np.pad(lb.mask.arr == -1, 1, constant_values=False)  # outside: not solid
+        cx = (0, 1, 0, -1, 0, 1, -1, -1, 1)
+        cy = (0, 0, 1, 0, -1, 1, 1, -1, -1)
+        opp = (0, 3, 4, 1, 2, 7, 8, 5, 6)
         rows = []
         active = (code & A.CODE_ACTIVE) != 0
         for kp in range(1, 9):
             k = opp[kp]
-            i2, j2 = I + cx[k], J + cy[k]
-            inside = (i2 >= 0) & (i2 < nx) & (j2 >= 0) & (j2 < ny)
-            solid = np.zeros_like(inside)
-            solid[inside] = mask[i2[inside], j2[inside]] == -1
-            sel = active & ((code >> (kp - 1)) & 1 == 1) & solid
-            ii, jj = I[sel], J[sel]
+            sel = active & (((code >> (kp - 1)) & 1) == 1) & \
+                solid[1 + cx[k]:1 + cx[k] + nx, 1 + cy[k]:1 + cy[k] + ny]
+            ii, jj = np.nonzero(sel)  # i-major, the order of the node grid
             rows.append(np.stack([jj * lb.pitch + ii, np.full_like(ii, k)], 1))
         links = np.concatenate(rows).astype(np.int32) if rows else np.zeros((0, 2), np.int32)
         t = torch.as_tensor(links if links.size else np.zeros((1, 2), np.int32), device=lb.device)
