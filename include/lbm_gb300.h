@@ -398,9 +398,14 @@ int lbm_batch_remove(LbmBatch* batch, int32_t slot);
 int lbm_batch_monitor(LbmBatch* batch, int32_t slot, const int32_t* links, int64_t nlinks, double* series,
                       int32_t* count, int32_t capacity);
 int lbm_batch_set_graph(LbmBatch* batch, int32_t enable);
+/* Members (other than Shan-Chen ones) of at least min_nodes lattice nodes
+ * run their own single-lattice step inside each batched step (the plan's
+ * lane-granular two-pass launch, parameters by value) instead of the packed
+ * tile table; 0 puts every member in the tables.  Default 2^19. */
+int lbm_batch_set_solo(LbmBatch* batch, int64_t min_nodes);
 int lbm_batch_run(LbmBatch* batch, int32_t nsteps, void* stream);
-/* members; tiles and groups of the current tables (-1 before the first run
- * after a change) */
+/* members; tiles and launch units (tile groups and solo members) of the
+ * current tables (-1 before the first run after a change) */
 int lbm_batch_info(const LbmBatch* batch, int32_t* members, int64_t* tiles, int32_t* groups);
 int lbm_batch_destroy(LbmBatch* batch);
 

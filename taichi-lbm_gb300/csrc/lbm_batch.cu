@@ -76,6 +76,14 @@ struct LbmBatch {
   bool use_graph = false;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
+  // members of at least solo_nodes nodes run their own single-lattice step
+  // (parameters by value, in the constant bank) instead of the packed tiles
+  int64_t solo_nodes = int64_t(1) << 19;
+  struct Solo {
+    int storage, V, flip;
+    lbm::FusedParams p[2];  // [parity]
+  };
+  std::vector<Solo> solos;
 };
 
 namespace {
@@ -100,23 +108,53 @@ int launch_monitors(LbmBatch* b, int sp, cudaStream_t s) {
   return LBM_OK;
 }
 
-// one batched step at parity sp on stream s: the groups on the worker
-// streams (forked from s and joined back), then the monitors on s
+int launch_solo(const LbmBatch::Solo& m, int sp, cudaStream_t s, cudaStream_t s2) {
+  const lbm::FusedParams& p = m.p[(sp ^ m.flip) & 1];
+  switch (m.storage) {
+    case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, m.V, s, s2);
+    case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, m.V, s, s2);
+    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, m.V, s, s2);
+  }
+}
+
+// streams a step's launches use: one per tile group, and per solo member one
+// for its segments plus one for its marked lanes (the two read the same
+// source and write disjoint nodes, so they overlap like the plan's own fork)
+int launch_slots(const LbmBatch* b) {
+  int n = (int)b->groups.size();
+  for (const LbmBatch::Solo& m : b->solos) n += m.p[0].nlanes > 0 ? 2 : 1;
+  return n;
+}
+
+// one batched step at parity sp on stream s: the groups and solo members on
+// the worker streams (forked from s and joined back), then the monitors on s
 int batch_step(LbmBatch* b, int sp, cudaStream_t s) {
-  const int ng = (int)b->groups.size();
-  if (ng <= 1) {
+  const int nslot = launch_slots(b);
+  if (nslot <= 1) {
     for (BatchGroup& g : b->groups) {
       int rc = launch_group(g, b->d_lats, b->d_tiles, sp, s);
       if (rc) return rc;
     }
+    for (const LbmBatch::Solo& m : b->solos) {
+      int rc = launch_solo(m, sp, s, s);
+      if (rc) return rc;
+    }
     return launch_monitors(b, sp, s);
   }
-  const int nw = ng < LbmBatch::NWORK ? ng : LbmBatch::NWORK;
+  const int nw = nslot < LbmBatch::NWORK ? nslot : LbmBatch::NWORK;
   int rc = lbm_err::cuda(cudaEventRecord(b->step_fork, s), "batch: step fork");
   for (int w = 0; !rc && w < nw; ++w) rc = lbm_err::cuda(cudaStreamWaitEvent(b->work[w], b->step_fork, 0), "batch: step fork");
   if (rc) return rc;
   int rl = LBM_OK;
-  for (int i = 0; i < ng && !rl; ++i) rl = launch_group(b->groups[i], b->d_lats, b->d_tiles, sp, b->work[i % nw]);
+  int k = 0;
+  for (size_t i = 0; i < b->groups.size() && !rl; ++i)
+    rl = launch_group(b->groups[i], b->d_lats, b->d_tiles, sp, b->work[k++ % nw]);
+  for (size_t i = 0; i < b->solos.size() && !rl; ++i) {
+    const LbmBatch::Solo& m = b->solos[i];
+    cudaStream_t a = b->work[k++ % nw];
+    cudaStream_t c = m.p[0].nlanes > 0 ? b->work[k++ % nw] : a;
+    rl = launch_solo(m, sp, a, c);
+  }
   // join every worker even after a failed launch
   for (int w = 0; w < nw; ++w) {
     int rj = lbm_err::cuda(cudaEventRecord(b->step_join[w], b->work[w]), "batch: step join");
@@ -191,6 +229,7 @@ int rebuild(LbmBatch* b) {
   std::map<GroupKey, std::vector<BatchTile>> by_key;  // references stay valid as keys are added
   auto bucket = [&](const GroupKey& k) -> std::vector<BatchTile>& { return by_key[k]; };
   std::vector<BatchMonitor> mons[3];
+  std::vector<LbmBatch::Solo> solos;
   // rows per Shan-Chen strip: the longest that still gives the GPU enough
   // strips in total (two per resident warp of 152 SMs x 12 warps)
   int sc_rows = 2 * lbm::SC_CHUNK;
@@ -219,9 +258,33 @@ int rebuild(LbmBatch* b) {
       rec.lean[v] = lbm::lean_of(rec.full[v]);
       rec.lean[v].sc_rows = sc_rows;
     }
-    pl->parity = saved;
     rec.flip = saved ^ sp;
     lats.push_back(rec);
+    if (!pl->d.sc && (int64_t)pl->d.nx * pl->d.ny >= b->solo_nodes && b->solo_nodes > 0 && pl->b.special &&
+        pl->b.lane_mask && pl->b.lanes && pl->d.pipeline == LBM_PIPE_DIRECT) {
+      LbmBatch::Solo so;
+      so.storage = pl->d.storage;
+      so.V = pl->d.nodes_per_thread;
+      so.flip = rec.flip;
+      for (int v = 0; v < 2; ++v) {
+        pl->parity = v;
+        so.p[v] = lbm_plan_params(pl);  // the plan's own lane-granular two-pass step
+      }
+      pl->parity = saved;
+      solos.push_back(so);
+      if (m.monitored) {
+        BatchMonitor bm;
+        bm.lat = lat;
+        bm.nlinks = m.nlinks;
+        bm.links = m.links;
+        bm.series = m.series;
+        bm.count = m.count;
+        bm.capacity = m.capacity;
+        mons[pl->d.storage].push_back(bm);
+      }
+      continue;
+    }
+    pl->parity = saved;
     const lbm::FusedParams& p = rec.full[0];
     const int pw = pl->d.fluid_model == LBM_POWERLAW ? 1 : 0;
     if (pl->d.sc) {
@@ -239,6 +302,7 @@ int rebuild(LbmBatch* b) {
         for (int l = 0; l < 32; ++l)
           if (mk >> l & 1u) ts.push_back({lat, item * 32 + l});
       }
+      while (tl.size() % lbm::BATCH_WARPS) tl.push_back({lat, -1});  // whole blocks per lattice
     }
     if (m.monitored) {
       BatchMonitor bm;
@@ -300,6 +364,7 @@ int rebuild(LbmBatch* b) {
   b->d_lats = T.lats;
   b->d_tiles = T.tiles;
   b->d_mons = T.mons;
+  b->solos = std::move(solos);
   b->ntiles = (long long)tiles.size();
   b->nlats = (int)lats.size();
   b->dirty = false;
@@ -439,6 +504,13 @@ int lbm_batch_remove(LbmBatch* b, int32_t slot) {
   return LBM_OK;
 }
 
+int lbm_batch_set_solo(LbmBatch* b, int64_t min_nodes) {
+  if (!b || min_nodes < 0) return lbm_err::set(LBM_ERR_ARG, "batch_set_solo: bad arguments");
+  b->solo_nodes = min_nodes;
+  b->dirty = true;
+  return LBM_OK;
+}
+
 int lbm_batch_set_graph(LbmBatch* b, int32_t enable) {
   if (!b) return lbm_err::set(LBM_ERR_ARG, "batch_set_graph: NULL batch");
   b->use_graph = enable != 0;
@@ -470,7 +542,7 @@ int lbm_batch_info(const LbmBatch* b, int32_t* members, int64_t* tiles, int32_t*
   for (const BatchMember& m : b->slots) n += m.plan ? 1 : 0;
   if (members) *members = n;
   if (tiles) *tiles = b->dirty ? -1 : b->ntiles;
-  if (groups) *groups = b->dirty ? -1 : (int32_t)b->groups.size();
+  if (groups) *groups = b->dirty ? -1 : (int32_t)(b->groups.size() + b->solos.size());
   return LBM_OK;
 }
 

@@ -7,9 +7,9 @@
 // kind an item is one row segment (y * nseg + seg), for the marked-lane kind
 // one lane ((y * nseg + seg) * 32 + lane), for Shan-Chen one
 // strip of 32V columns and SC_CHUNK rows (chunk * nseg + seg).  The kernels
-// are persistent: a grid sized to the GPU walks the table, a warp per tile,
-// and copies a lattice's parameters into the warp's shared memory when its
-// tile belongs to another lattice than the previous one.  Tables are ordered by lattice,
+// for the segment kinds run one warp per tile; the Shan-Chen strips are
+// persistent (a grid sized to the GPU walks the table, a warp per tile).  A
+// warp copies its lattice's parameters into its shared memory.  Tables are ordered by lattice,
 // then row, so consecutive tiles touch neighbouring memory.
 #pragma once
 
@@ -33,34 +33,33 @@ __device__ __forceinline__ int view_of(const BatchLattice* lats, int lat, int sp
 
 constexpr int BATCH_WARPS = 8;  // warps per block of the segment kinds
 
-// Plain segments of every lattice in the table.
+// Plain-path segments of every lattice in the table: one warp per tile (the
+// hardware balances the blocks, so work that runs beside this kernel on
+// other streams never leaves a statically assigned share behind).  Every
+// lattice's tiles are padded to whole blocks (item -1), so a block serves one
+// lattice and stages its parameters in shared memory once.
 template <int MODEL, bool PL, int ST, int V, int FORCE>
 __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLattice* __restrict__ lats,
                                                                   const BatchTile* __restrict__ tiles, int ntiles,
                                                                   int sp) {
-  __shared__ LeanParams lp[BATCH_WARPS];
+  __shared__ LeanParams p;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  LeanParams& p = lp[warp];
-  int cur = -1;
-  for (int t = blockIdx.x * BATCH_WARPS + warp; t < ntiles; t += gridDim.x * BATCH_WARPS) {
-    const BatchTile tile = tiles[t];
-    if (tile.lat != cur) {
-      __syncwarp();
-      copy_words(&p, &lats[tile.lat].lean[view_of(lats, tile.lat, sp)], lane, 32);
-      __syncwarp();
-      cur = tile.lat;
-    }
-    const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
-    const int seg = tile.item - y * p.nseg;
-    const int x0s = seg * 32 * V, x0 = x0s + lane * V;
-    uint32_t mask;  // lanes k_batch_lanes stores
-    ldg_early(p.lane_mask + tile.item, mask);
-    float h[V][9];
-    if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
-    else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
-    if (mask == 0xffffffffu) continue;
-    lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0, (mask >> lane) & 1u);
-  }
+  const int t0 = blockIdx.x * BATCH_WARPS;
+  const int lat = tiles[t0].lat;
+  copy_words(&p, &lats[lat].lean[view_of(lats, lat, sp)], threadIdx.x, BATCH_WARPS * 32);
+  __syncthreads();
+  const BatchTile tile = tiles[t0 + warp];
+  if (tile.item < 0) return;
+  const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
+  const int seg = tile.item - y * p.nseg;
+  const int x0s = seg * 32 * V, x0 = x0s + lane * V;
+  uint32_t mask;  // lanes k_batch_lanes stores
+  ldg_early(p.lane_mask + tile.item, mask);
+  float h[V][9];
+  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
+  else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
+  if (mask == 0xffffffffu) return;
+  lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0, (mask >> lane) & 1u);
 }
 
 // Marked lanes (bounce-back links, boundary programs, saved moments,
@@ -190,9 +189,7 @@ int launch_batch_seg(BatchGroup& g, const BatchLattice* lats, const BatchTile* t
     return lbm_err::launch("batched step (marked lanes)");
   }
   auto kern = g.force ? k_batch_lean<MODEL, PL, ST, V, 1> : k_batch_lean<MODEL, PL, ST, V, 0>;
-  const int b = batch_grid(kern, BATCH_WARPS * 32, BATCH_WARPS, g.count, &g.blocks);
-  if (b <= 0) return b < 0 ? b : lbm_err::set(LBM_ERR_ARG, "batch: empty grid");
-  kern<<<b, BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
+  kern<<<(unsigned)((g.count + BATCH_WARPS - 1) / BATCH_WARPS), BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
   return lbm_err::launch("batched step (plain segments)");
 }
 

@@ -223,17 +223,18 @@ __device__ __forceinline__ void shifted_feq(const P& p, float rho, float ux, flo
   const float rs = SCALED ? rho * sc : rho;
   const float r0 = rs * W(0), r1 = rs * W(1), r2 = rs * W(5);
   const float a1 = 3.0f * r1, a2 = 3.0f * r2;
-  float w[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) w[k] = SCALED ? p.wsh[k] * sc : p.wsh[k];
-  e[0] = fmaf(r0, base, -w[0]);
+  // the shift has three distinct weights (rest, axis, diagonal)
+  const float w0 = SCALED ? p.wsh[0] * sc : p.wsh[0];
+  const float w1 = SCALED ? p.wsh[1] * sc : p.wsh[1];
+  const float w2 = SCALED ? p.wsh[5] * sc : p.wsh[5];
+  e[0] = fmaf(r0, base, -w0);
   const float eu[4] = {ux, uy, ux + uy, uy - ux};  // c.u of k = 1, 2, 5, 6
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int k = q < 2 ? q + 1 : q + 3;
     const float r = q < 2 ? r1 : r2, a = q < 2 ? a1 : a2;
     const float t = fmaf(4.5f * eu[q], eu[q], base);
-    const float sym = fmaf(r, t, -w[k]);
+    const float sym = fmaf(r, t, -(q < 2 ? w1 : w2));
     const float anti = a * eu[q];
     e[k] = sym + anti;
     e[OPP(k)] = sym - anti;
@@ -378,7 +379,8 @@ __device__ __forceinline__ float collide_lean(const P& p, float h[9], float stat
     }
 #pragma unroll
     for (int a = 0; a < 9; ++a) {
-      float v = fmaf(-s[a], m[a] - (meq[a] - p.mwsh[a]), m[a]);
+      // M wsh vanishes beyond the first three moments (the shift is at rest)
+      float v = fmaf(-s[a], m[a] - (a < 3 ? meq[a] - p.mwsh[a] : meq[a]), m[a]);
       if (FORCE) v = fmaf(1.0f - 0.5f * s[a], mf[a], v);
       m[a] = v;
     }

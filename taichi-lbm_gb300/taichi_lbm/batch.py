@@ -22,12 +22,17 @@ from .lbm import stream_handle
 
 
 class Batch:
-    def __init__(self, graphs=True):
+    def __init__(self, graphs=True, solo_nodes=None):
+        """solo_nodes: members of at least this many nodes run their own
+        single-lattice step inside each batched step (lbm_batch_set_solo);
+        None keeps the library default, 0 packs every member."""
         h = ctypes.c_void_p()
         A.call("lbm_batch_create", ctypes.byref(h))
         self._h = h
         self.graphs = bool(graphs)
         A.call("lbm_batch_set_graph", self._h, 1 if self.graphs else 0)
+        if solo_nodes is not None:
+            A.call("lbm_batch_set_solo", self._h, int(solo_nodes))
         self.members = {}  # slot -> (solver, monitor tensors or None)
 
     @staticmethod

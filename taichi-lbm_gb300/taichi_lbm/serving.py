@@ -83,7 +83,8 @@ class Server:
     """builders: host threads that build arriving requests' lattices (each
     on its own CUDA stream) while the scheduler keeps the GPU busy."""
 
-    def __init__(self, tl, hbm_budget, graphs=True, slice_steps=200, keep_fields=False, builders=1):
+    def __init__(self, tl, hbm_budget, graphs=True, slice_steps=200, keep_fields=False, builders=1, ahead=2,
+                 reserve_bytes=16 << 30):
         self.tl = tl
         self.batch = Batch(graphs=graphs)
         self.budget = int(hbm_budget)
@@ -91,6 +92,8 @@ class Server:
         self.slice_steps = int(slice_steps)
         self.keep_fields = keep_fields
         self.builders = max(1, int(builders))
+        self.ahead = max(1, int(ahead))  # slices queued on the GPU before the scheduler waits
+        self.reserve_bytes = int(reserve_bytes)
         self.queue = collections.deque()
         self.active = {}        # slot -> [request, solver, remaining steps, bytes]
         self.done = []
@@ -161,11 +164,26 @@ class Server:
 
         pending = collections.deque(sorted(self.queue, key=lambda r: r.arrival))
         self.queue.clear()
-        streams = [torch.cuda.Stream() for _ in range(self.builders)]
-        self.retire_stream = torch.cuda.Stream()
+        # builders' and retirement's short kernels go ahead of the batch's
+        # persistent ones: high stream priority
+        hi = torch.cuda.Stream.priority_range()[1] if hasattr(torch.cuda.Stream, "priority_range") else -1
+        streams = [torch.cuda.Stream(priority=hi) for _ in range(self.builders)]
+        self.retire_stream = torch.cuda.Stream(priority=hi)
+        # lattices of every size come and go: give each builder stream one
+        # large cached segment up front, so building carves tensors out of it
+        # instead of calling the driver allocator per tensor
+        reserve = min(self.budget, self.reserve_bytes) // self.builders
+        for st in streams:
+            with torch.cuda.stream(st):
+                del_me = torch.empty(reserve, dtype=torch.uint8, device="cuda")
+                del del_me
         building = collections.deque()  # (request, future) in admission order
         retiring = []                   # members that left, with the event to wait for
-        with cf.ThreadPoolExecutor(self.builders) as pool:
+        inflight = collections.deque()  # end events of the slices queued on the GPU
+        # the scheduler's own stream: nothing implicit (work on the legacy
+        # default stream from any thread) queues behind the batch's slices
+        sched = torch.cuda.Stream()
+        with cf.ThreadPoolExecutor(self.builders) as pool, torch.cuda.stream(sched):
             n_started = 0
             while pending or building or self.active or retiring:
                 t = now()
@@ -183,8 +201,15 @@ class Server:
                 self._leave(retiring)  # single-step requests
                 launched = False
                 if self.active:
+                    # at most `ahead` slices queued: the scheduler (and the
+                    # builders' small GPU steps) stay close to the GPU's clock
+                    while len(inflight) >= self.ahead:
+                        inflight.popleft().synchronize()
                     k = min(self.slice_steps, min(a[2] for a in self.active.values()))
                     self.batch.run(k)
+                    ev = torch.cuda.Event()
+                    ev.record()
+                    inflight.append(ev)
                     launched = True
                     for a in self.active.values():
                         a[2] -= k

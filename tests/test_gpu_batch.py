@@ -3,7 +3,8 @@ its result alone (FusedSolver.step on its own), whatever the mix of
 collision models, storages, body forces, power law, Shan-Chen tiles and
 lattice sizes; members may join and leave between runs (at either ping-pong
 parity); graph replay equals direct launches; the batched drag/lift monitor
-equals the per-lattice one.
+equals the per-lattice one; members run as solo single-lattice steps inside
+the batch give the same results as packed ones.
 """
 import numpy as np
 import pytest
@@ -89,11 +90,14 @@ def check_same(got, ref, storage, keys=("rho", "vel", "f")):
         assert rel_err(got[k], ref[k]) <= TOL[storage], (k, rel_err(got[k], ref[k]))
 
 
+@pytest.mark.parametrize("solo", [None, 1])
 @pytest.mark.parametrize("graphs", [False, True])
-def test_mix_equals_alone(tl, graphs):
+def test_mix_equals_alone(tl, graphs, solo):
+    """solo=1: every member with special work runs its own single-lattice
+    step inside the batched step instead of the packed tiles."""
     n = 40
     refs = {k: alone(tl, k, n) for k in KINDS}
-    batch = tl.Batch(graphs=graphs)
+    batch = tl.Batch(graphs=graphs, solo_nodes=solo)
     solvers = {}
     for k in KINDS:
         factory, _ = make(tl, k)
@@ -154,11 +158,12 @@ def test_graph_replay_equals_direct_launches(tl):
             assert rel_err(x[k], y[k]) == 0.0, k
 
 
-def test_batched_monitor_equals_plan_series(tl):
+@pytest.mark.parametrize("solo", [None, 1])
+def test_batched_monitor_equals_plan_series(tl, solo):
     n = 30
     lb, me, coll, be = cylinder_channel(tl, 200, 60, 6.0, 40.0, 29.5, 0.6, 0.05)
     ref = tl.FusedSolver(lb, me, coll, be).step(n, forces=True).cpu().numpy()
-    batch = tl.Batch(graphs=True)
+    batch = tl.Batch(graphs=True, solo_nodes=solo)
     lb, me, coll, be = cylinder_channel(tl, 200, 60, 6.0, 40.0, 29.5, 0.6, 0.05)
     s = tl.FusedSolver(lb, me, coll, be)
     other = make(tl, "cyl_trt_f16")[0]()
