@@ -391,7 +391,7 @@ def run_ours(a):
                      "algorithmic_bytes_per_launch": BYTES_PER_LU[a.storage] * active,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel": ("one fused step: k_fused_bulk (every segment, marked lanes skipped) + k_fused_lanes "
-                                "(flagged segments), timed together"
+                                "(marked lanes, side stream), timed together"
                                 if solver.launches_per_step == 2 else "one fused step (one launch)")},
         "clocks": clocks,
         "e2e": {"value": round(active * K * ws / e2e_dt / 1e6, 1), "unit": METRIC,
