@@ -248,12 +248,21 @@ def run_batched(tl, storage, K, W, gpu_index, graphs=True):
     Returns aggregate MLUPS over every lattice and the roofline figures."""
     import torch
     from taichi_lbm.workloads import batched_shan_chen
+    # autotune nodes per thread and strip rows on a sample of the same lattices
+    t0 = time.perf_counter()
+    tuner = tl.Autotuner(steps=30, warmup=5)
+
+    def sample(V):
+        return [tl.FusedSolver(lb, me, coll, be, storage=storage, sc_boundary_engine=bsc, nodes_per_thread=V)
+                for lb, me, coll, be, sc, bsc in batched_shan_chen(tl, count=12)]
+    V, _, rows = tuner.batch_shape(f"sc-batch/{storage}", sample, storage, graphs=graphs, sc=True)
+    tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     cases = batched_shan_chen(tl)
-    solvers = [tl.FusedSolver(lb, me, coll, be, storage=storage, sc_boundary_engine=bsc)
+    solvers = [tl.FusedSolver(lb, me, coll, be, storage=storage, sc_boundary_engine=bsc, nodes_per_thread=V)
                for lb, me, coll, be, sc, bsc in cases]
     nodes = sum(c[0].NX * c[0].NY for c in cases)
-    batch = tl.Batch(graphs=graphs)
+    batch = tl.Batch(graphs=graphs, sc_rows=rows)
     for s in solvers:
         batch.add(s)
     setup = time.perf_counter() - t0
@@ -281,6 +290,9 @@ def run_batched(tl, storage, K, W, gpu_index, graphs=True):
             "steps": K, "ms_per_step": round(ms / K, 4), "lattices": 64, "nodes": nodes,
             "groups": info["groups"], "tiles": info["tiles"], "graphs": graphs,
             "setup_s": round(setup, 1), "finite_lattices": finite,
+            "autotune": {"nodes_per_thread": V, "sc_rows": rows, "seconds": round(tune_s, 1),
+                         "sample": "first 12 lattices of the same seeded draw",
+                         "trials": [{"cand": c, "ms_per_step": round(ms, 4)} for _, c, ms in tuner.trials]},
             "note": "lattices at T/Tc below about 0.78 diverge within a few hundred steps; the CPU oracle "
                     "of the reference's algorithm diverges on them alike, so the count is physics",
             "clocks": clk.summary()}
@@ -300,7 +312,20 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
     mean_work = sum(r.nodes * r.steps for r in probe) / n
     rate = 0.8 * capacity_mlups * 1e6 / mean_work
     reqs = request_stream(n, rate, storage=storage)
-    srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=200, builders=4)
+    # autotune (before the stream starts): nodes per thread per model at three
+    # lattice sizes, and the batch's solo threshold on a sample of the stream
+    t0 = time.perf_counter()
+    tuner = tl.Autotuner(steps=30, warmup=5)
+    from taichi_lbm.serving import Request
+    for model in ("bgk", "trt", "mrt"):
+        for nx in (256, 1024, 2048):
+            r = Request(0, nx, nx // 4, model, 0.55, 100, storage=storage)
+            tuner.nodes_per_thread(r.tune_key(), storage, lambda V, r=r: r.build(tl, nodes_per_thread=V))
+    tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=tuner.lookup(r.tune_key(), "V"))
+                                           for r in reqs[:16]], storage, tune_v=False)
+    tune_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()
+    srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=200, builders=4, autotuner=tuner)
     for r in reqs:
         srv.submit(r)
     with Clocks(gpu_index) as clk:
@@ -325,7 +350,11 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
                 "alone_fp32_MLUPS": round(alone_lu / alone_s / 1e6, 1),
                 "alone_sample": f"first {sample_alone} requests of the same stream, fp32, FusedSolver.step with "
                                 "drag/lift, one after another",
-                "clocks": clk.summary()})
+                "clocks": clk.summary(),
+                "autotune": {"seconds": round(tune_s, 1), "table": tuner.table,
+                             "what": "nodes per thread per model at 256/1024/2048 x NX/4 (nearest size bucket "
+                                     "used per request) and the batch's solo threshold on the first 16 "
+                                     "requests, each candidate timed with CUDA events over 30 steps"}})
     out["vs_alone_fp32"] = round(out["MLUPS"] / out["alone_fp32_MLUPS"], 3)
     return out
 

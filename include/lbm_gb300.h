@@ -403,6 +403,10 @@ int lbm_batch_set_graph(LbmBatch* batch, int32_t enable);
  * lane-granular two-pass launch, parameters by value) instead of the packed
  * tile table; 0 puts every member in the tables.  Default 2^19. */
 int lbm_batch_set_solo(LbmBatch* batch, int64_t min_nodes);
+/* Rows per Shan-Chen strip (the strip tile is 32 x nodes-per-thread columns
+ * by rows): 8, 16 or 32, or 0 for the default (the longest strips that
+ * still give every SM several). */
+int lbm_batch_set_sc_rows(LbmBatch* batch, int32_t rows);
 int lbm_batch_run(LbmBatch* batch, int32_t nsteps, void* stream);
 /* members; tiles and launch units (tile groups and solo members) of the
  * current tables (-1 before the first run after a change) */

@@ -79,6 +79,8 @@ struct LbmBatch {
   // members of at least solo_nodes nodes run their own single-lattice step
   // (parameters by value, in the constant bank) instead of the packed tiles
   int64_t solo_nodes = int64_t(1) << 19;
+  // rows per Shan-Chen strip (8, 16 or 32); 0 chooses from the batch's size
+  int sc_rows_fixed = 0;
   struct Solo {
     int storage, V, flip;
     lbm::FusedParams p[2];  // [parity]
@@ -232,8 +234,8 @@ int rebuild(LbmBatch* b) {
   std::vector<LbmBatch::Solo> solos;
   // rows per Shan-Chen strip: the longest that still gives the GPU enough
   // strips in total (two per resident warp of 152 SMs x 12 warps)
-  int sc_rows = 2 * lbm::SC_CHUNK;
-  for (; sc_rows > lbm::SC_CHUNK / 2; sc_rows /= 2) {
+  int sc_rows = b->sc_rows_fixed ? b->sc_rows_fixed : 2 * lbm::SC_CHUNK;
+  for (; !b->sc_rows_fixed && sc_rows > lbm::SC_CHUNK / 2; sc_rows /= 2) {
     long long items = 0;
     for (const BatchMember& m : b->slots)
       if (m.plan && m.plan->d.sc)
@@ -507,6 +509,15 @@ int lbm_batch_remove(LbmBatch* b, int32_t slot) {
 int lbm_batch_set_solo(LbmBatch* b, int64_t min_nodes) {
   if (!b || min_nodes < 0) return lbm_err::set(LBM_ERR_ARG, "batch_set_solo: bad arguments");
   b->solo_nodes = min_nodes;
+  b->dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_set_sc_rows(LbmBatch* b, int32_t rows) {
+  if (!b || (rows != 0 && rows != lbm::SC_CHUNK / 2 && rows != lbm::SC_CHUNK && rows != 2 * lbm::SC_CHUNK))
+    return lbm_err::set(LBM_ERR_ARG, "batch_set_sc_rows: rows must be 0, %d, %d or %d", lbm::SC_CHUNK / 2,
+                        lbm::SC_CHUNK, 2 * lbm::SC_CHUNK);
+  b->sc_rows_fixed = rows;
   b->dirty = true;
   return LBM_OK;
 }

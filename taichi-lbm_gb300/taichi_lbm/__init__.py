@@ -23,6 +23,7 @@ from .post import PostProcessingEngine
 from .solver import FusedSolver
 from .batch import Batch
 from .serving import Request, Server
+from .autotune import Autotuner
 from ._plan import UnsupportedComposition
 
 _capi.load()

@@ -22,10 +22,11 @@ from .lbm import stream_handle
 
 
 class Batch:
-    def __init__(self, graphs=True, solo_nodes=None):
+    def __init__(self, graphs=True, solo_nodes=None, sc_rows=None):
         """solo_nodes: members of at least this many nodes run their own
         single-lattice step inside each batched step (lbm_batch_set_solo);
-        None keeps the library default, 0 packs every member."""
+        None keeps the library default, 0 packs every member.  sc_rows: rows
+        per Shan-Chen strip (8, 16, 32; None chooses from the batch)."""
         h = ctypes.c_void_p()
         A.call("lbm_batch_create", ctypes.byref(h))
         self._h = h
@@ -33,6 +34,8 @@ class Batch:
         A.call("lbm_batch_set_graph", self._h, 1 if self.graphs else 0)
         if solo_nodes is not None:
             A.call("lbm_batch_set_solo", self._h, int(solo_nodes))
+        if sc_rows is not None:
+            A.call("lbm_batch_set_sc_rows", self._h, int(sc_rows))
         self.members = {}  # slot -> (solver, monitor tensors or None)
 
     @staticmethod

@@ -54,14 +54,19 @@ class Request:
     def latency(self):
         return None if self.finished is None else self.finished - self.arrival
 
-    def build(self, tl, keep_init=False):
+    def tune_key(self):
+        """Autotuner table key of this request's shape."""
+        from .autotune import Autotuner
+        return Autotuner.key(self.model, self.storage, self.nodes, powerlaw=self.powerlaw is not None)
+
+    def build(self, tl, keep_init=False, nodes_per_thread=None):
         """The request's lattice and solver (cylinder_channel + FusedSolver)."""
         r = self.ny / 10.0
         s = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1.0 / self.tau, 1.0 / self.tau] if self.model == "mrt" else None
         lb, me, coll, be = cylinder_channel(tl, self.nx, self.ny, r, self.nx / 5.0, self.ny / 2.0 - 0.5, self.tau,
                                             self.umax, model=self.model, mrt_s=s, keep_init=keep_init,
                                             name=f"req{self.rid}", powerlaw=self.powerlaw)
-        return tl.FusedSolver(lb, me, coll, be, storage=self.storage)
+        return tl.FusedSolver(lb, me, coll, be, storage=self.storage, nodes_per_thread=nodes_per_thread)
 
 
 def device_bytes(nx, ny, storage):
@@ -84,9 +89,13 @@ class Server:
     on its own CUDA stream) while the scheduler keeps the GPU busy."""
 
     def __init__(self, tl, hbm_budget, graphs=True, slice_steps=200, keep_fields=False, builders=1, ahead=2,
-                 reserve_bytes=16 << 30):
+                 reserve_bytes=16 << 30, autotuner=None, batch_key="served"):
+        """autotuner: an Autotuner whose table gives each request's nodes per
+        thread (by Request.tune_key) and the batch's shape (entry
+        `batch_key`); shapes it has no entry for keep the defaults."""
         self.tl = tl
-        self.batch = Batch(graphs=graphs)
+        self.autotuner = autotuner
+        self.batch = Batch(graphs=graphs, **(autotuner.batch_kwargs(batch_key) if autotuner else {}))
         self.budget = int(hbm_budget)
         self.used = 0
         self.slice_steps = int(slice_steps)
@@ -107,8 +116,9 @@ class Server:
     def _build(self, req, stream):
         """Builder thread: lattice, plan, first step and first drag/lift row
         on `stream`; returns what the scheduler needs to join the batch."""
+        V = self.autotuner.lookup(req.tune_key(), "V") if self.autotuner else None
         with torch.cuda.stream(stream):
-            solver = req.build(self.tl)
+            solver = req.build(self.tl, nodes_per_thread=V)
             mon = Batch.prepare(solver, req.steps)
             ev = torch.cuda.Event()
             ev.record(stream)

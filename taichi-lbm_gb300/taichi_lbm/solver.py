@@ -16,6 +16,7 @@ collision runs through the per-stage kernels, then n-1 fused launches (each
 and boundary pass and the moment kernels.
 """
 import ctypes
+import zlib
 
 import numpy as np
 import torch
@@ -327,6 +328,63 @@ class FusedSolver:
     def sync(self):
         if getattr(self, "_live", False):
             self.finish()
+
+    # ------------------------------------------------------------ checkpoint / resume
+    CHECKPOINT_FORMAT = "taichi_lbm.fused.v1"
+
+    def _fingerprint(self):
+        """What a checkpoint must match: lattice shape, storage, model and the
+        compiled node codes (geometry and boundary programs)."""
+        d = self.desc
+        return {"nx": int(d.nx), "ny": int(d.ny), "pitch": int(d.pitch), "storage": int(self.storage),
+                "model": int(d.model), "fluid_model": int(d.fluid_model), "sc": int(d.sc),
+                "code_crc": zlib.crc32(np.ascontiguousarray(self.compiled.code).tobytes())}
+
+    def _state_buffers(self):
+        # the two ping-pong buffers in bind order (fa, fb)
+        return list(self.fbuf) if self.fbuf is not None else [self.lb._f2, self.lb._f]
+
+    def checkpoint(self):
+        """Snapshot of a live run (between begin() and finish()) as CPU tensors:
+        both population buffers in their storage type (the 16-bit shifted
+        values as stored, so nothing is rounded twice), both saved-moment
+        buffers, the per-node relaxation state of a power-law run, the
+        ping-pong parity and LBField.time.  torch.save() writes it to disk;
+        restore() on a solver built for the same lattice resumes from it, and
+        the resumed run equals the uninterrupted one to the bit.  Queued work
+        on the current stream finishes first (the copies are ordered after it)."""
+        if not getattr(self, "_live", False):
+            raise RuntimeError("checkpoint() needs a live run (between begin() and finish())")
+        ck = {"format": self.CHECKPOINT_FORMAT, "plan": self._fingerprint(), "parity": self.parity_now(),
+              "f": [b.detach().cpu().clone() for b in self._state_buffers()],
+              "mom": [m.detach().cpu().clone() for m in self.mom],
+              "tau": self.tau_state.detach().cpu().clone() if self.powerlaw else None,
+              "time": self.lb.time[None]}
+        return ck
+
+    def restore(self, ck):
+        """Resume a run from checkpoint() output (or its torch.load()): binds
+        this solver's buffers, loads the state and leaves the run live, as
+        begin() does; continue with run(n) / a Batch, then finish()."""
+        if not isinstance(ck, dict) or ck.get("format") != self.CHECKPOINT_FORMAT:
+            raise ValueError("not a fused-solver checkpoint")
+        if ck["plan"] != self._fingerprint():
+            raise ValueError(f"checkpoint is for another lattice or plan: {ck['plan']} != {self._fingerprint()}")
+        if getattr(self, "_live", False):
+            raise RuntimeError("restore() on a live run; finish() it first")
+        self._bind()
+        for dst, src in zip(self._state_buffers(), ck["f"]):
+            if dst.shape != src.shape or dst.dtype != src.dtype:
+                raise ValueError("checkpoint buffer shape or type differs")
+            dst.copy_(src)
+        for dst, src in zip(self.mom, ck["mom"]):
+            dst.copy_(src)
+        if self.powerlaw:
+            self.tau_state.copy_(ck["tau"])
+        A.call("lbm_plan_set_parity", self._plan, int(ck["parity"]))
+        self.lb.time[None] = ck["time"]
+        self.lb._fused_owner = self
+        self._live = True
 
     def parity_now(self):
         """0: the live state is in the first buffer (f2's storage for fp32)."""

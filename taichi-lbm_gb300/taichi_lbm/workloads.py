@@ -3,13 +3,14 @@
 cylinder_channel: the reference's cylinder case (cases/Circular cylinder.py)
 as a channel with walls on every lattice edge, with boundary groups that
 never index outside the lattice, and a parabolic inlet given per node through
-BoundarySpec.value_fn.
+BoundarySpec.value_fn.  contraction_channel: the planar contraction of
+cases/contraction flow.py with a power-law fluid.
 """
 import numpy as np
 
 
 def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=None, magic=0.25,
-                     name="cylinder", keep_init=True, powerlaw=None):
+                     name="cylinder", keep_init=True, powerlaw=None, tau_clamp=None):
     """Channel with a cylinder: walls on every lattice edge (bounce-back for
     every missing link), periodic stream carrier, parabolic VelocityEquilibrium
     inlet at i = 0 (direction 3), PressureNEEM outlet rho = 1 at i = NX-1
@@ -19,6 +20,37 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
     lb.keep_init_snapshot = keep_init
     be = tl.BoundaryEngine()
     be.Mask_cricle_identify(lb, cx, cy, radius)
+    return _channel(tl, lb, be, nx, ny, tau, umax, 0, ny, model, mrt_s, magic, powerlaw, tau_clamp)
+
+
+def contraction_channel(tl, nx=2048, ny=512, outlet_h=128, n=1.0, re=20.0, umax=0.02, model="trt",
+                        tau_clamp=(0.505, 2.0), magic=0.25, name="contraction", keep_init=False):
+    """Planar contraction (the reference's cases/contraction flow.py, scaled):
+    a channel of height NY whose second half (x >= NX/2) is closed above and
+    below by solid, leaving an outlet section `outlet_h` high in the middle
+    (two Mask_rectangle_identify rectangles).  Parabolic inlet of peak `umax`
+    over the full height, PressureNEEM outlet, bounce-back walls, power-law
+    fluid of index n with the consistency m of Reynolds number `re` on the
+    outlet height (m = umax^(2-n) outlet_h^n / Re, as cases/Power Law
+    Fluid.py:41 relates K to Re), relaxation time clamped to `tau_clamp`.
+    The initial tau is that of the nominal shear rate umax / outlet_h."""
+    lb = tl.LBField(name, nx, ny, 1)
+    lb.keep_init_snapshot = keep_init
+    be = tl.BoundaryEngine()
+    lo, hi = (ny - outlet_h) // 2, (ny + outlet_h) // 2
+    # open rectangles: x in (nx/2 - 1, nx + 1), y in (-1, lo) and (hi - 1, ny + 1)
+    be.Mask_rectangle_identify(lb, nx // 2 - 1, nx + 1, -1, lo)
+    be.Mask_rectangle_identify(lb, nx // 2 - 1, nx + 1, hi - 1, ny + 1)
+    m = umax ** (2.0 - n) * float(outlet_h) ** n / re
+    nu0 = m * (umax / outlet_h) ** (n - 1.0)
+    tau = min(max(0.5 + 3.0 * nu0, tau_clamp[0]), tau_clamp[1])
+    return _channel(tl, lb, be, nx, ny, tau, umax, 0, ny, model, None, magic, (m, n), tau_clamp)
+
+
+def _channel(tl, lb, be, nx, ny, tau, umax, y0, y1, model, mrt_s, magic, powerlaw, tau_clamp):
+    """Boundary groups and collision of a channel whose solid is already in
+    lb.mask: bounce-back for every missing link, periodic carrier, parabolic
+    inlet over rows [y0, y1) at i = 0, PressureNEEM outlet at i = NX-1."""
     cls = tl.BoundaryClassifier((nx, ny))
     mask = lb.mask.arr
     fluid_arr = mask == 1
@@ -30,6 +62,7 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
         ex, ey = int(lb.c[k, 0]), int(lb.c[k, 1])
         missing |= ~src_ok[1 - ex:1 - ex + nx, 1 - ey:1 - ey + ny]
     wall_arr = fluid_arr & missing
+    h = float(y1 - y0)
 
     def fluid_fn(i, j):
         return fluid_arr[i, j]
@@ -44,8 +77,8 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
         return fluid_arr[i, j] & (i == nx - 1)
 
     def parabola(i, j):
-        y = j + 0.5
-        return (4.0 * umax * y * (ny - y) / (ny * ny), np.zeros(np.shape(j)))
+        y = np.clip(j + 0.5 - y0, 0.0, h)
+        return (4.0 * umax * y * (h - y) / (h * h), np.zeros(np.shape(j)))
 
     fluid = tl.FluidBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
     fluid.precompute(classifier=cls)
@@ -69,6 +102,8 @@ def cylinder_channel(tl, nx, ny, radius, cx, cy, tau, umax, model="bgk", mrt_s=N
     fluid_model = tl.NewtonianFluid(nu=nu) if powerlaw is None else tl.PowerLawFluid(*powerlaw)
     params = {"group": fluid.group, "fluid_model": fluid_model, "NX": nx, "NY": ny,
               "num_components": 1, "shearviscosity": [nu], "magic": [magic], "bulkviscosity": [nu]}
+    if tau_clamp is not None:
+        params["tau_clamp"] = tau_clamp
     if model == "bgk":
         coll = tl.BGKCollision(params)
     elif model == "trt":
