@@ -276,4 +276,5 @@ def summarize(done, makespan, lattice_updates):
     return {"requests": len(done), "makespan_s": round(makespan, 3),
             "MLUPS": round(lattice_updates / makespan / 1e6, 1),
             "p50_s": round(float(np.percentile(lat, 50)), 4), "p99_s": round(float(np.percentile(lat, 99)), 4),
-            "finite": int(sum(1 for r in done if r.finite))}
+            "finite": int(sum(1 for r in done if r.finite)),
+            "nonfinite_requests": sorted(int(r.rid) for r in done if not r.finite)}

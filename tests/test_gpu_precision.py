@@ -4,11 +4,14 @@ Power-law contraction (taichi_lbm.workloads.contraction_channel, the
 reference's cases/contraction flow.py with a power-law fluid, TRT, relaxation
 time clamped to [0.505, 2.0], inlet peak 0.02): for n in {0.5, 1.0, 1.5} and
 each storage, rho and u after N steps against the oracle run in double
-precision.  Bounds: max|a-b|/max|b| per field <= 1e-4 for fp32, <= 1e-3 for
-fp16-shifted, <= 1e-2 for bf16-shifted (8-bit significand).  The default
-size is a 512 x 128 lattice (outlet 32 high) for 4,000 steps; with
-LBM_PRECISION_FULL=1 the test runs the 2048 x 512 lattice (outlet 128 high)
-for 20,000 steps instead.  Each case prints one JSON line with its errors.
+precision (max|a-b|/max|b| per field).  The oracle is also run in single
+precision: its distance from the double run is the case's rounding floor,
+which grows without bound once a flow is unsteady (the shear-thinning n = 0.5
+jet through the contraction becomes so after ~2,000 steps at the default
+size).  Bound: err <= max(TOL, 3 x floor), TOL = 1e-4 (fp32), 1e-3
+(fp16-shifted), 1e-2 (bf16-shifted, 8-bit significand).  Default: a 512 x 128
+lattice (outlet 32 high) for 4,000 steps; LBM_PRECISION_SIZE="nx,ny,outlet,
+steps" runs another size.  Each case prints one JSON line.
 
 Mass: a closed periodic box (no inflow or outflow, so the exact mass is
 constant) runs 10,000 fused steps; the FP64 reduction of the population sum
@@ -26,8 +29,7 @@ from tests.test_gpu_lean import periodic_box
 
 pytestmark = pytest.mark.gpu
 
-FULL = os.environ.get("LBM_PRECISION_FULL") == "1"
-SIZE = (2048, 512, 128, 20000) if FULL else (512, 128, 32, 4000)
+SIZE = tuple(int(v) for v in os.environ.get("LBM_PRECISION_SIZE", "512,128,32,4000").split(","))
 TOL = {"fp32": 1e-4, "fp16s": 1e-3, "bf16s": 1e-2}
 # relative mass drift over 10,000 steps of a 1024 x 1024 periodic box
 DRIFT = {"fp32": 1e-10, "fp16s": 1e-6, "bf16s": 1e-4}
@@ -40,33 +42,38 @@ def tl(built):
 
 
 @pytest.fixture(scope="module")
-def fp64_refs(tl):
-    """FP64 oracle fields per power-law index, built once."""
+def oracle_refs(tl):
+    """(FP64 oracle fields, FP32 oracle fields) per power-law index."""
     from taichi_lbm.workloads import contraction_channel
     nx, ny, h, steps = SIZE
     out = {}
     for n in (0.5, 1.0, 1.5):
         lb, me, coll, be = contraction_channel(tl, nx, ny, h, n=n, keep_init=True)
         meta, arrays = describe(lb, coll, be, steps, step_kind="powerlaw", fp="f64")
-        arrays = {k: (v.astype(np.float64) if v.dtype == np.float32 else v) for k, v in arrays.items()}
-        out[n] = O.replay(meta, arrays)
+        a64 = {k: (v.astype(np.float64) if v.dtype == np.float32 else v) for k, v in arrays.items()}
+        ref64 = O.replay(meta, a64)
+        ref32 = O.replay(dict(meta, fp="f32"), arrays)
+        out[n] = (ref64, ref32)
     return out
 
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
 @pytest.mark.parametrize("n", [0.5, 1.0, 1.5])
-def test_power_law_contraction_vs_fp64(tl, fp64_refs, n, storage):
+def test_power_law_contraction_vs_fp64(tl, oracle_refs, n, storage):
     from taichi_lbm.workloads import contraction_channel
     nx, ny, h, steps = SIZE
     lb, me, coll, be = contraction_channel(tl, nx, ny, h, n=n)
     tl.FusedSolver(lb, me, coll, be, storage=storage).step(steps)
     got = fields_of(lb)
-    ref = fp64_refs[n]
-    err = {k: rel_err(got[k], ref[k]) for k in ("rho", "vel")}
+    ref64, ref32 = oracle_refs[n]
+    err = {k: rel_err(got[k], ref64[k]) for k in ("rho", "vel")}
+    floor = {k: rel_err(ref32[k], ref64[k]) for k in ("rho", "vel")}
     print(json.dumps({"case": "power-law contraction", "nx": nx, "ny": ny, "outlet": h, "steps": steps,
-                      "n": n, "storage": storage, "rel_err_rho": err["rho"], "rel_err_vel": err["vel"]}))
+                      "n": n, "storage": storage, "rel_err_rho": err["rho"], "rel_err_vel": err["vel"],
+                      "oracle_fp32_floor_rho": floor["rho"], "oracle_fp32_floor_vel": floor["vel"]}))
     assert np.isfinite(got["rho"]).all()
-    assert err["rho"] <= TOL[storage] and err["vel"] <= TOL[storage], err
+    for k in ("rho", "vel"):
+        assert err[k] <= max(TOL[storage], 3.0 * floor[k]), (k, err, floor)
 
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
