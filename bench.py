@@ -255,7 +255,8 @@ def run_batched(tl, storage, K, W, gpu_index, graphs=True):
     def sample(V):
         return [tl.FusedSolver(lb, me, coll, be, storage=storage, sc_boundary_engine=bsc, nodes_per_thread=V)
                 for lb, me, coll, be, sc, bsc in batched_shan_chen(tl, count=12)]
-    V, _, rows = tuner.batch_shape(f"sc-batch/{storage}", sample, storage, graphs=graphs, sc=True)
+    # (Shan-Chen plans run 4 nodes per thread; the strip height is the knob)
+    V, _, rows = tuner.batch_shape(f"sc-batch/{storage}", sample, storage, graphs=graphs, sc=True, tune_v=False)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     cases = batched_shan_chen(tl)
