@@ -38,7 +38,7 @@ for _p in (PKG, ROOT):
 
 METRIC = "MLUPS"
 # algorithmic bytes per lattice update: 9 populations read + 9 written
-BYTES_PER_LU = {"fp32": 72, "fp16s": 36, "bf16s": 36}
+BYTES_PER_LU = {"fp32": 72, "fp16s": 36, "bf16s": 36, "i16s": 36}
 CONFIG = {"nx": 8192, "ny": 2048, "radius": 200.0, "cx": 1600.0, "cy": 1024.0, "tau": 0.52,
           "umax": 0.04}
 MRT_S = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1.0 / 0.52, 1.0 / 0.52]
@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--model", default="bgk", choices=["bgk", "trt", "mrt"])
-    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "bf16s"])
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "bf16s", "i16s"])
     ap.add_argument("--nx", type=int, default=CONFIG["nx"])
     ap.add_argument("--ny", type=int, default=CONFIG["ny"])
     ap.add_argument("--nodes-per-thread", type=int, default=None)
@@ -435,7 +435,7 @@ def run_ours(a):
     torch.cuda.empty_cache()
     if not a.no_extras and ws == 1:
         extras = {}
-        for model, storage in (("trt", "fp32"), ("mrt", "fp32"), ("bgk", "fp16s"), ("bgk", "bf16s")):
+        for model, storage in (("trt", "fp32"), ("mrt", "fp32"), ("bgk", "fp16s"), ("bgk", "bf16s"), ("bgk", "i16s")):
             if (model, storage) == (a.model, a.storage):
                 continue
             lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None, a.pipeline)

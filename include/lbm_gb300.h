@@ -53,8 +53,11 @@ enum {
 enum { LBM_BGK = 0, LBM_TRT = 1, LBM_MRT = 2 };
 /* fluid models (taichi_lbm/FluidModels.py) */
 enum { LBM_NEWTONIAN = 0, LBM_POWERLAW = 1 };
-/* population storage for the fused path */
-enum { LBM_STORE_F32 = 0, LBM_STORE_F16S = 1, LBM_STORE_BF16S = 2 };
+/* population storage for the fused path: fp32; fp16 / bf16 shifted; int16
+ * fixed point shifted (steps of 2^-19, |f_k - w_k rho_ref| < 1/16, every
+ * collision conserves each node's stored mass exactly; direct and prefetch
+ * pipelines, not Shan-Chen) */
+enum { LBM_STORE_F32 = 0, LBM_STORE_F16S = 1, LBM_STORE_BF16S = 2, LBM_STORE_I16S = 3 };
 /* pseudopotentials (taichi_lbm/EOS.py) */
 enum { LBM_EOS_SC = 0, LBM_EOS_VDW = 1, LBM_EOS_RK = 2, LBM_EOS_PR = 3, LBM_EOS_CS = 4 };
 /* boundary-condition kinds (taichi_lbm/BoundaryCondition.py) */
@@ -253,7 +256,7 @@ typedef struct LbmPlanDesc {
   float g_coh;
   float sc_T;
   LbmEos eos;
-  /* 16-bit storages (LBM_STORE_F16S / BF16S) hold f_k - w_k * rho_ref so the
+  /* 16-bit storages (LBM_STORE_F16S / BF16S / I16S) hold f_k - w_k * rho_ref so the
    * stored value is the small deviation from rest at density rho_ref; choose
    * the lattice's mean density (0 is read as 1).  Ignored for fp32.        */
   float rho_ref;

@@ -26,6 +26,7 @@
 LBM_BATCH_EXTERN(LBM_STORE_F32)
 LBM_BATCH_EXTERN(LBM_STORE_F16S)
 LBM_BATCH_EXTERN(LBM_STORE_BF16S)
+LBM_BATCH_EXTERN(LBM_STORE_I16S)
 
 using lbm::BatchGroup;
 using lbm::BatchLattice;
@@ -69,7 +70,7 @@ struct LbmBatch {
   cudaStream_t work[NWORK] = {};
   cudaEvent_t step_fork = nullptr;
   cudaEvent_t step_join[NWORK] = {};
-  int mon_off[3] = {0, 0, 0}, mon_cnt[3] = {0, 0, 0};  // monitors per storage
+  int mon_off[4] = {0, 0, 0, 0}, mon_cnt[4] = {0, 0, 0, 0};  // monitors per storage
   long long ntiles = 0;
   int nlats = 0;
   // graphs
@@ -94,17 +95,19 @@ int launch_group(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles
   switch (g.storage) {
     case LBM_STORE_F32: return lbm::launch_batch_group<LBM_STORE_F32>(g, lats, tiles, sp, s);
     case LBM_STORE_F16S: return lbm::launch_batch_group<LBM_STORE_F16S>(g, lats, tiles, sp, s);
-    default: return lbm::launch_batch_group<LBM_STORE_BF16S>(g, lats, tiles, sp, s);
+    case LBM_STORE_BF16S: return lbm::launch_batch_group<LBM_STORE_BF16S>(g, lats, tiles, sp, s);
+    default: return lbm::launch_batch_group<LBM_STORE_I16S>(g, lats, tiles, sp, s);
   }
 }
 
 int launch_monitors(LbmBatch* b, int sp, cudaStream_t s) {
-  for (int st = 0; st < 3; ++st) {
+  for (int st = 0; st < 4; ++st) {
     if (!b->mon_cnt[st]) continue;
     const BatchMonitor* m = b->d_mons + b->mon_off[st];
-    int rc = st == LBM_STORE_F32    ? lbm::launch_batch_monitors<LBM_STORE_F32>(b->d_lats, m, b->mon_cnt[st], sp, s)
-             : st == LBM_STORE_F16S ? lbm::launch_batch_monitors<LBM_STORE_F16S>(b->d_lats, m, b->mon_cnt[st], sp, s)
-                                    : lbm::launch_batch_monitors<LBM_STORE_BF16S>(b->d_lats, m, b->mon_cnt[st], sp, s);
+    int rc = st == LBM_STORE_F32     ? lbm::launch_batch_monitors<LBM_STORE_F32>(b->d_lats, m, b->mon_cnt[st], sp, s)
+             : st == LBM_STORE_F16S  ? lbm::launch_batch_monitors<LBM_STORE_F16S>(b->d_lats, m, b->mon_cnt[st], sp, s)
+             : st == LBM_STORE_BF16S ? lbm::launch_batch_monitors<LBM_STORE_BF16S>(b->d_lats, m, b->mon_cnt[st], sp, s)
+                                     : lbm::launch_batch_monitors<LBM_STORE_I16S>(b->d_lats, m, b->mon_cnt[st], sp, s);
     if (rc) return rc;
   }
   return LBM_OK;
@@ -115,7 +118,8 @@ int launch_solo(const LbmBatch::Solo& m, int sp, cudaStream_t s, cudaStream_t s2
   switch (m.storage) {
     case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, m.V, s, s2);
     case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, m.V, s, s2);
-    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, m.V, s, s2);
+    case LBM_STORE_BF16S: return lbm::launch_fused<LBM_STORE_BF16S>(p, m.V, s, s2);
+    default: return lbm::launch_fused<LBM_STORE_I16S>(p, m.V, s, s2);
   }
 }
 
@@ -230,7 +234,7 @@ int rebuild(LbmBatch* b) {
   std::vector<BatchLattice> lats;
   std::map<GroupKey, std::vector<BatchTile>> by_key;  // references stay valid as keys are added
   auto bucket = [&](const GroupKey& k) -> std::vector<BatchTile>& { return by_key[k]; };
-  std::vector<BatchMonitor> mons[3];
+  std::vector<BatchMonitor> mons[4];
   std::vector<LbmBatch::Solo> solos;
   // rows per Shan-Chen strip: the longest that still gives the GPU enough
   // strips in total (two per resident warp of 152 SMs x 12 warps)
@@ -339,7 +343,7 @@ int rebuild(LbmBatch* b) {
   }
   if (tiles.size() > (size_t)INT32_MAX) return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch: too many tiles");
   std::vector<BatchMonitor> allm;
-  for (int st = 0; st < 3; ++st) {
+  for (int st = 0; st < 4; ++st) {
     b->mon_off[st] = (int)allm.size();
     b->mon_cnt[st] = (int)mons[st].size();
     allm.insert(allm.end(), mons[st].begin(), mons[st].end());

@@ -174,6 +174,73 @@ struct Storage<LBM_STORE_BF16S> {
   static __device__ __forceinline__ T enc(float v, float w) { return __float2bfloat16_rn(v - w); }
 };
 
+// 16-bit fixed point, shifted (LBM_STORE_I16S): the state holds the integer
+// n = round((f_k - w_k rho_ref) / Q), Q = 2^-19, as int16, so |f_k - w_k
+// rho_ref| < 2^15 Q = 1/16.  Every stored value is a multiple of Q below
+// 2^15 Q, so a sum of a node's nine values is exact in FP32 (9 * 2^15 <
+// 2^24): a collision can store its populations with their sum, the node's
+// mass, unchanged to the bit (i16_conserve), which floating-point storage
+// cannot.  Rounding is to nearest even through the 1.5 * 2^23 magic
+// constant (x + 1.5 * 2^23 rounds x to an integer for |x| < 2^22); values
+// outside the range saturate.
+constexpr float I16_Q = 1.9073486328125e-06f;  // 2^-19
+constexpr float I16_IQ = 524288.0f;            // 2^19
+constexpr float I16_MAGIC = 12582912.0f;       // 1.5 * 2^23
+
+// the nearest step count of a shifted value, saturated, as an integer float
+__device__ __forceinline__ float i16_steps(float h) {
+  const float n = fmaf(h, I16_IQ, I16_MAGIC) - I16_MAGIC;
+  return fminf(fmaxf(n, -32768.0f), 32767.0f);
+}
+// an integer float in [-32768, 32767] -> its int16 bits (in the low half)
+__device__ __forceinline__ unsigned i16_bits(float n) { return __float_as_uint(n + I16_MAGIC) & 0xffffu; }
+
+template <>
+struct Storage<LBM_STORE_I16S> {
+  using T = short;
+  static __device__ __forceinline__ float dec(T v, float w) { return fmaf((float)v, I16_Q, w); }
+  static __device__ __forceinline__ double dec64(T v, float w) { return (double)v * (double)I16_Q + (double)w; }
+  static __device__ __forceinline__ T enc(float v, float w) { return (short)i16_bits(i16_steps(v - w)); }
+};
+
+// Mass-conserving quantisation of one node's post-collision populations
+// for the fixed-point storage: populations 1..8 round to their nearest
+// step, and population 0 takes the rest of the node's pre-collision mass
+// d (a sum of stored values, exact), so the stored sum equals d exactly.
+// h: shifted post-collision values; on return, multiples of Q.
+__device__ __forceinline__ void i16_conserve(float (&h)[9], float d) {
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 1; k < 9; ++k) {
+    const float n = i16_steps(h[k]);
+    s += n;  // exact: integers below 2^24
+    h[k] = n * I16_Q;
+  }
+  const float n0 = fminf(fmaxf(fmaf(d, I16_IQ, -s), -32768.0f), 32767.0f);
+  h[0] = n0 * I16_Q;
+}
+
+// The general (unshifted) path holds f = n Q + w rounded to FP32; the nearest
+// step of f - w recovers n exactly (the FP32 rounding is far below Q / 2).
+// i16_mass: a node's stored sum from its unshifted values (exact), and
+// i16_store_node: the conserving quantisation of a node's post-collision f
+// as int16 step counts.
+__device__ __forceinline__ float i16_mass(const float (&f)[9], const float (&w)[9]) {
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s += i16_steps(f[k] - w[k]);
+  return s * I16_Q;
+}
+__device__ __forceinline__ void i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
+                                               short (&out)[9]) {
+  float h[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) h[k] = f[k] - w[k];
+  i16_conserve(h, mass);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) out[k] = (short)i16_bits(h[k] * I16_IQ);
+}
+
 template <int BYTES>
 struct Raw;
 template <>
@@ -549,9 +616,11 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   }
   const bool force = FORCE < 0 ? p.has_force != 0 : FORCE == 1;
   const float Fx = force ? p.gx : 0.0f, Fy = force ? p.gy : 0.0f;
+  float mass[V];  // fixed-point storage: each node's stored sum before the collision
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     float* fi = f[i];
+    if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh);
     const float rho = ((fi[0] + fi[1]) + (fi[2] + fi[3])) + ((fi[4] + fi[5]) + (fi[6] + fi[7])) + fi[8];
     const float jx = (fi[1] - fi[3]) + (fi[5] - fi[6]) + (fi[8] - fi[7]);
     const float jy = (fi[2] - fi[4]) + (fi[5] + fi[6]) - (fi[7] + fi[8]);
@@ -569,6 +638,7 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
       if (live) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), p.wsh[k]);
+        if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh);
       }
     } else if (PL) {
       tau[i] = st;
@@ -577,6 +647,19 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
+  if constexpr (ST == LBM_STORE_I16S) {
+    short q[V][9];
+#pragma unroll
+    for (int i = 0; i < V; ++i) i16_store_node(f[i], p.wsh, mass[i], q[i]);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      T raw[V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) raw[i] = q[i][k];
+      store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
+    }
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     T raw[V];
@@ -616,6 +699,8 @@ __device__ __forceinline__ void lane_general(const FusedParams& p, int y, int x0
       if (bi < 0) break;
       apply_bc<ST>(p, bi, x, y, f);
     }
+    float mass = 0.0f;  // fixed-point storage: the node's stored sum before the collision
+    if constexpr (ST == LBM_STORE_I16S) mass = i16_mass(f, p.wsh);
     const float rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
     const float jx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
     const float jy = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
@@ -627,8 +712,15 @@ __device__ __forceinline__ void lane_general(const FusedParams& p, int y, int x0
     }
     const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
     if (PL) p.tau[q] = st;
+    if constexpr (ST == LBM_STORE_I16S) {
+      short n[9];
+      i16_store_node(f, p.wsh, mass, n);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k]);
+      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = n[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k]);
+    }
   }
 }
 

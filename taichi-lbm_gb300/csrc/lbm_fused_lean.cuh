@@ -25,6 +25,18 @@ template <>
 __device__ __forceinline__ float raw_to_float<LBM_STORE_F16S>(__half v) { return __half2float(v); }
 template <>
 __device__ __forceinline__ float raw_to_float<LBM_STORE_BF16S>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <>
+__device__ __forceinline__ float raw_to_float<LBM_STORE_I16S>(short v) { return (float)v * I16_Q; }
+
+// two int16 step counts packed in a word -> their shifted values, without
+// an integer conversion: 0x4B00xxxx with xxxx = n + 2^15 is the float
+// 2^23 + 2^15 + n, and (that - 2^23 - 2^15) * Q is n * Q, exact in one fma
+__device__ __forceinline__ float2 i16_pair_to_floats(unsigned w) {
+  const unsigned u = w ^ 0x80008000u;
+  const float lo = __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7610));
+  const float hi = __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7632));
+  return make_float2(fmaf(lo, I16_Q, -16.0625f), fmaf(hi, I16_Q, -16.0625f));
+}
 
 // V stored values -> floats (no shift)
 template <int ST, int V>
@@ -41,12 +53,21 @@ __device__ __forceinline__ void raw_to_floats(const typename Storage<ST>::T (&ra
       c[i] = u.x;
       c[i + 1] = u.y;
     }
-  } else {
+  } else if constexpr (ST == LBM_STORE_BF16S) {
 #pragma unroll
     for (int i = 0; i < V; i += 2) {
       __nv_bfloat162 t;
       memcpy(&t, &raw[i], sizeof(t));
       const float2 u = __bfloat1622float2(t);
+      c[i] = u.x;
+      c[i + 1] = u.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < V; i += 2) {
+      unsigned w;
+      memcpy(&w, &raw[i], sizeof(w));
+      const float2 u = i16_pair_to_floats(w);
       c[i] = u.x;
       c[i + 1] = u.y;
     }
@@ -122,11 +143,17 @@ __device__ __forceinline__ void store_raw(typename Storage<ST>::T* p, const floa
       const __half2 t = __floats2half2_rn(c[i], c[i + 1]);
       memcpy(&raw[i], &t, sizeof(t));
     }
-  } else {
+  } else if constexpr (ST == LBM_STORE_BF16S) {
 #pragma unroll
     for (int i = 0; i < V; i += 2) {
       const __nv_bfloat162 t = __floats2bfloat162_rn(c[i], c[i + 1]);
       memcpy(&raw[i], &t, sizeof(t));
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < V; i += 2) {
+      const unsigned w = __byte_perm(i16_bits(i16_steps(c[i])), i16_bits(i16_steps(c[i + 1])), 0x5410);
+      memcpy(&raw[i], &w, sizeof(w));
     }
   }
   store_vec<T, V>(p, raw);
@@ -430,6 +457,11 @@ __device__ __forceinline__ float collide_lean(const P& p, float h[9], float stat
   return state;
 }
 
+// sum of a node's nine shifted values (exact for the fixed-point storage)
+__device__ __forceinline__ float node_sum(const float (&h)[9]) {
+  return ((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7])) + h[8];
+}
+
 // Moments, collision and stores of one lane's V nodes (x0.., row y) of a
 // plain segment, from the gathered stored values h.
 template <class P, int MODEL, bool PL, int ST, int V, int FORCE>
@@ -446,10 +478,16 @@ __device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9],
       for (int i = 0; i < V; ++i) tau[i] = 1.0f;
     }
   }
+  float mass[V];  // fixed-point storage: each node's stored sum before the collision (exact)
+  if constexpr (ST == LBM_STORE_I16S) {
+#pragma unroll
+    for (int i = 0; i < V; ++i) mass[i] = node_sum(h[i]);
+  }
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     const float st = collide_lean<P, MODEL, PL, FORCE>(p, h[i], PL ? tau[i] : 0.0f);
     if (PL) tau[i] = st;
+    if constexpr (ST == LBM_STORE_I16S) i16_conserve(h[i], mass[i]);
   }
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);

@@ -9,6 +9,7 @@
 LBM_EXTERN_STORAGE(LBM_STORE_F32)
 LBM_EXTERN_STORAGE(LBM_STORE_F16S)
 LBM_EXTERN_STORAGE(LBM_STORE_BF16S)
+LBM_EXTERN_STORAGE(LBM_STORE_I16S)
 
 namespace {
 
@@ -50,20 +51,23 @@ int dispatch_fused(const FusedParams& p, int st, int V, cudaStream_t s, cudaStre
     switch (st) {
       case LBM_STORE_F32: return lbm::launch_fused_sc<LBM_STORE_F32>(p, s);
       case LBM_STORE_F16S: return lbm::launch_fused_sc<LBM_STORE_F16S>(p, s);
-      default: return lbm::launch_fused_sc<LBM_STORE_BF16S>(p, s);
+      case LBM_STORE_BF16S: return lbm::launch_fused_sc<LBM_STORE_BF16S>(p, s);
+      default: return lbm::launch_fused_sc<LBM_STORE_I16S>(p, s);
     }
   }
   if (pipeline == LBM_PIPE_ASYNC || (pipeline == LBM_PIPE_PREFETCH && !p.plain)) {
     switch (st) {
       case LBM_STORE_F32: return lbm::launch_fused_persistent<LBM_STORE_F32>(p, pipeline, tune, status, s);
       case LBM_STORE_F16S: return lbm::launch_fused_persistent<LBM_STORE_F16S>(p, pipeline, tune, status, s);
-      default: return lbm::launch_fused_persistent<LBM_STORE_BF16S>(p, pipeline, tune, status, s);
+      case LBM_STORE_BF16S: return lbm::launch_fused_persistent<LBM_STORE_BF16S>(p, pipeline, tune, status, s);
+      default: return lbm::launch_fused_persistent<LBM_STORE_I16S>(p, pipeline, tune, status, s);
     }
   }
   switch (st) {
     case LBM_STORE_F32: return lbm::launch_fused<LBM_STORE_F32>(p, V, s, s2);
     case LBM_STORE_F16S: return lbm::launch_fused<LBM_STORE_F16S>(p, V, s, s2);
-    default: return lbm::launch_fused<LBM_STORE_BF16S>(p, V, s, s2);
+    case LBM_STORE_BF16S: return lbm::launch_fused<LBM_STORE_BF16S>(p, V, s, s2);
+    default: return lbm::launch_fused<LBM_STORE_I16S>(p, V, s, s2);
   }
 }
 
@@ -137,7 +141,7 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   if (d->model < LBM_BGK || d->model > LBM_MRT) return lbm_err::set(LBM_ERR_ARG, "model %d", d->model);
   if (d->fluid_model != LBM_NEWTONIAN && d->fluid_model != LBM_POWERLAW)
     return lbm_err::set(LBM_ERR_ARG, "fluid model %d", d->fluid_model);
-  if (d->storage < LBM_STORE_F32 || d->storage > LBM_STORE_BF16S)
+  if (d->storage < LBM_STORE_F32 || d->storage > LBM_STORE_I16S)
     return lbm_err::set(LBM_ERR_ARG, "storage %d", d->storage);
   const int V = d->nodes_per_thread;
   const bool vok = d->storage == LBM_STORE_F32 ? (V == 2 || V == 4) : (V == 4 || V == 8);
@@ -147,6 +151,10 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   if (d->pipeline != LBM_PIPE_DIRECT && V != lbm::AV && !(d->pipeline == LBM_PIPE_PREFETCH && V == 8))
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "persistent pipelines run %d nodes per thread (prefetch: also 8 "
                         "with 16-bit storage)", lbm::AV);
+  if (d->sc && d->storage == LBM_STORE_I16S)  // phase separation leaves the +-1/16 range of the steps
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans store fp32, fp16 or bf16 populations");
+  if (d->pipeline == LBM_PIPE_ASYNC && d->storage == LBM_STORE_I16S)
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "the fixed-point storage runs the direct or prefetch pipeline");
   if (d->pipeline == LBM_PIPE_ASYNC && (d->tune < 0 || d->tune >= LBM_ASYNC_TUNINGS))
     return lbm_err::set(LBM_ERR_ARG, "async tuning %d", d->tune);
   if (d->pipeline == LBM_PIPE_PREFETCH && (d->tune < 0 || d->tune >= LBM_PREFETCH_TUNINGS))
@@ -284,7 +292,8 @@ int lbm_plan_stream(LbmPlan* pl, float* f_out, void* stream) {
   switch (pl->d.storage) {
     case LBM_STORE_F32: return lbm::launch_stream_only<LBM_STORE_F32>(p, f_out, s);
     case LBM_STORE_F16S: return lbm::launch_stream_only<LBM_STORE_F16S>(p, f_out, s);
-    default: return lbm::launch_stream_only<LBM_STORE_BF16S>(p, f_out, s);
+    case LBM_STORE_BF16S: return lbm::launch_stream_only<LBM_STORE_BF16S>(p, f_out, s);
+    default: return lbm::launch_stream_only<LBM_STORE_I16S>(p, f_out, s);
   }
 }
 
@@ -302,8 +311,11 @@ static int convert(LbmPlan* pl, const float* in, float* out, void* stream) {
   if (pl->d.storage == LBM_STORE_F16S)
     return in ? lbm::launch_convert<LBM_STORE_F16S>(p, in, cur, 1, s)
               : lbm::launch_convert<LBM_STORE_F16S>(p, nullptr, out, 0, s);
-  return in ? lbm::launch_convert<LBM_STORE_BF16S>(p, in, cur, 1, s)
-            : lbm::launch_convert<LBM_STORE_BF16S>(p, nullptr, out, 0, s);
+  if (pl->d.storage == LBM_STORE_BF16S)
+    return in ? lbm::launch_convert<LBM_STORE_BF16S>(p, in, cur, 1, s)
+              : lbm::launch_convert<LBM_STORE_BF16S>(p, nullptr, out, 0, s);
+  return in ? lbm::launch_convert<LBM_STORE_I16S>(p, in, cur, 1, s)
+            : lbm::launch_convert<LBM_STORE_I16S>(p, nullptr, out, 0, s);
 }
 
 int lbm_plan_import(LbmPlan* pl, const float* f_post, void* stream) {
@@ -327,7 +339,8 @@ static int mex(LbmPlan* pl, const int32_t* links, int64_t n, double* out, cudaSt
   switch (pl->d.storage) {
     case LBM_STORE_F32: return lbm::launch_momentum_exchange<LBM_STORE_F32>(p, links, n, out, s);
     case LBM_STORE_F16S: return lbm::launch_momentum_exchange<LBM_STORE_F16S>(p, links, n, out, s);
-    default: return lbm::launch_momentum_exchange<LBM_STORE_BF16S>(p, links, n, out, s);
+    case LBM_STORE_BF16S: return lbm::launch_momentum_exchange<LBM_STORE_BF16S>(p, links, n, out, s);
+    default: return lbm::launch_momentum_exchange<LBM_STORE_I16S>(p, links, n, out, s);
   }
 }
 
@@ -465,7 +478,8 @@ int lbm_plan_reduce_moments_noalloc(LbmPlan* pl, double* out, void* stream) {
   switch (pl->d.storage) {
     case LBM_STORE_F32: return launch_noalloc<LBM_STORE_F32>(p, partials, nblocks, out, s);
     case LBM_STORE_F16S: return launch_noalloc<LBM_STORE_F16S>(p, partials, nblocks, out, s);
-    default: return launch_noalloc<LBM_STORE_BF16S>(p, partials, nblocks, out, s);
+    case LBM_STORE_BF16S: return launch_noalloc<LBM_STORE_BF16S>(p, partials, nblocks, out, s);
+    default: return launch_noalloc<LBM_STORE_I16S>(p, partials, nblocks, out, s);
   }
 }
 
@@ -479,7 +493,8 @@ int lbm_plan_reduce_moments(LbmPlan* pl, double* partials, double* out, void* st
   switch (pl->d.storage) {
     case LBM_STORE_F32: return lbm::launch_reduce<LBM_STORE_F32>(p, partials, out, s);
     case LBM_STORE_F16S: return lbm::launch_reduce<LBM_STORE_F16S>(p, partials, out, s);
-    default: return lbm::launch_reduce<LBM_STORE_BF16S>(p, partials, out, s);
+    case LBM_STORE_BF16S: return lbm::launch_reduce<LBM_STORE_BF16S>(p, partials, out, s);
+    default: return lbm::launch_reduce<LBM_STORE_I16S>(p, partials, out, s);
   }
 }
 

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "liblbm_gb300.so")
 LBM_OK = 0
 BGK, TRT, MRT = 0, 1, 2
 NEWTONIAN, POWERLAW = 0, 1
-STORE_F32, STORE_F16S, STORE_BF16S = 0, 1, 2
+STORE_F32, STORE_F16S, STORE_BF16S, STORE_I16S = 0, 1, 2, 3
 EOS_SC, EOS_VDW, EOS_RK, EOS_PR, EOS_CS = 0, 1, 2, 3, 4
 BC_FLUID, BC_VELOCITY_BB, BC_VELOCITY_EQ, BC_VELOCITY_NEEM = 0, 1, 2, 3
 BC_PRESSURE_ABC, BC_PRESSURE_NEEM, BC_OPEN_NEUMANN, BC_OPEN_CONV1 = 4, 5, 6, 7

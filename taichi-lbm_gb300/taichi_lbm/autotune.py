@@ -20,7 +20,7 @@ import os
 
 import torch
 
-V_CANDIDATES = {"fp32": (2, 4), "fp16s": (4, 8), "bf16s": (4, 8)}
+V_CANDIDATES = {"fp32": (2, 4), "fp16s": (4, 8), "bf16s": (4, 8), "i16s": (4, 8)}
 SC_ROWS = (8, 16, 32)
 SOLO_CANDIDATES = (0, 1 << 18, 1 << 19, 1 << 20, 1 << 62)
 

@@ -27,8 +27,11 @@ from .boundary import BoundaryCondition
 from .collision import BGKCollision, MRTCollision, PowerLawFluid, TRTCollision
 from .lbm import stream_handle
 
-STORAGE = {"fp32": A.STORE_F32, "fp16s": A.STORE_F16S, "bf16s": A.STORE_BF16S}
-DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 4, A.STORE_BF16S: 4}
+# "i16s": int16 fixed point (steps of 2^-19) of f - w_k rho_ref; every
+# collision conserves each node's stored mass exactly
+STORAGE = {"fp32": A.STORE_F32, "fp16s": A.STORE_F16S, "bf16s": A.STORE_BF16S, "i16s": A.STORE_I16S}
+DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 4, A.STORE_BF16S: 4, A.STORE_I16S: 4}
+STATE_DTYPE = {A.STORE_F16S: torch.float16, A.STORE_BF16S: torch.bfloat16, A.STORE_I16S: torch.int16}
 PIPELINE = {"direct": A.PIPE_DIRECT, "async": A.PIPE_ASYNC, "prefetch": A.PIPE_PREFETCH}
 
 
@@ -211,8 +214,7 @@ class FusedSolver:
         if self.storage == A.STORE_F32:
             self.fbuf = None
         else:
-            self.fbuf = [torch.zeros((9, ny, P), dtype=torch.float16 if self.storage == A.STORE_F16S
-                                     else torch.bfloat16, device=dev) for _ in range(2)]
+            self.fbuf = [torch.zeros((9, ny, P), dtype=STATE_DTYPE[self.storage], device=dev) for _ in range(2)]
         plan = ctypes.c_void_p()
         A.call("lbm_plan_create", ctypes.byref(d), ctypes.byref(plan))
         self._plan = plan

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 MRT_S = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1 / 0.56, 1 / 0.56]
 # same kernels' arithmetic in both forms; the bound allows for a different
 # fma contraction of the same expressions
-TOL = {"fp32": 1e-5, "fp16s": 1e-3, "bf16s": 1e-2}
+TOL = {"fp32": 1e-5, "fp16s": 1e-3, "bf16s": 1e-2, "i16s": 1e-3}
 
 
 @pytest.fixture(scope="module")
@@ -44,6 +44,11 @@ def make(tl, kind):
                                                 mrt_s=MRT_S)
             return tl.FusedSolver(lb, me, coll, be, storage="bf16s")
         return f, "bf16s"
+    if kind == "cyl_trt_i16":
+        def f():
+            lb, me, coll, be = cylinder_channel(tl, 416, 64, 6.4, 83.2, 31.5, 0.56, 0.05, model="trt")
+            return tl.FusedSolver(lb, me, coll, be, storage="i16s", nodes_per_thread=8)
+        return f, "i16s"
     if kind == "box_mrt_gravity_f32":
         def f():
             lb, me, coll, be = periodic_box(tl, "mrt", tl.NewtonianFluid(0.05), True, nx=389, ny=40)
@@ -73,8 +78,8 @@ def make(tl, kind):
     raise KeyError(kind)
 
 
-KINDS = ["cyl_bgk_f32", "cyl_trt_f16", "cyl_mrt_bf16", "box_mrt_gravity_f32", "box_trt_powerlaw_f32",
-         "box_bgk_v2_f32", "sc_bgk_f32", "sc_bgk_f16"]
+KINDS = ["cyl_bgk_f32", "cyl_trt_f16", "cyl_mrt_bf16", "cyl_trt_i16", "box_mrt_gravity_f32",
+         "box_trt_powerlaw_f32", "box_bgk_v2_f32", "sc_bgk_f32", "sc_bgk_f16"]
 
 
 def alone(tl, kind, n):

@@ -42,7 +42,7 @@ def factory(tl, kind):
     return make(tl, kind)[0]
 
 
-@pytest.mark.parametrize("kind", ["cyl_bgk_f32", "cyl_mrt_f16", "box_trt_powerlaw_bf16", "sc_bgk_f16"])
+@pytest.mark.parametrize("kind", ["cyl_bgk_f32", "cyl_mrt_f16", "box_trt_powerlaw_bf16", "sc_bgk_f16", "cyl_trt_i16"])
 def test_resume_equals_uninterrupted(tl, kind, tmp_path):
     f = factory(tl, kind)
     a = f()

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 # 520 columns: five 128-node segments at 4 nodes per lane, three of them interior
 NX, NY = 520, 24
-STORE_TOL = {"fp16s": 2e-3, "bf16s": 2e-2}
+STORE_TOL = {"fp16s": 2e-3, "bf16s": 2e-2, "i16s": 2e-3}
 MRT_S = [0.0, 1.64, 1.54, 0.0, 1.7, 0.0, 1.7, 1 / 0.65, 1 / 0.65]
 
 
@@ -68,7 +68,7 @@ def check_storage(got, ref64, storage):
 
 @pytest.mark.parametrize("pipeline", ["direct", "prefetch"])
 @pytest.mark.parametrize("gravity", [False, True])
-@pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s", "i16s"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
 def test_lean_periodic_box(tl, model, storage, gravity, pipeline):
     lb, me, coll, be = periodic_box(tl, model, tl.NewtonianFluid(0.05), gravity)
@@ -84,7 +84,7 @@ def test_lean_periodic_box(tl, model, storage, gravity, pipeline):
 
 
 @pytest.mark.parametrize("pipeline", ["direct", "prefetch"])
-@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "i16s"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
 def test_lean_periodic_box_power_law(tl, model, storage, pipeline):
     lb, me, coll, be = periodic_box(tl, model, tl.PowerLawFluid(0.02, 0.7), True)
@@ -97,7 +97,7 @@ def test_lean_periodic_box_power_law(tl, model, storage, pipeline):
         check_storage(got, fp64_solution(meta, arrays), storage)
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "i16s"])
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
 def test_two_pass_forms_agree(tl, model, storage):
     """One general launch, the two launches serialised, and the two launches
@@ -143,7 +143,7 @@ def test_prefetch_tunings_match_direct(tl, tune, shape):
         assert rel_err(out[1][k], out[0][k]) == 0.0, k
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "i16s"])
 @pytest.mark.parametrize("shape", [(520, 64), (200, 48)])
 def test_lane_special_equals_segment_special(tl, storage, shape):
     """Special work per lane (the plain kernel on every segment, one thread
