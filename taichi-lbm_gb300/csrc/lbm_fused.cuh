@@ -179,7 +179,7 @@ struct Storage<LBM_STORE_BF16S> {
 // rho_ref| < 2^15 Q = 1/16.  Every stored value is a multiple of Q below
 // 2^15 Q, so a sum of a node's nine values is exact in FP32 (9 * 2^15 <
 // 2^24): a collision can store its populations with their sum, the node's
-// mass, unchanged to the bit (i16_conserve), which floating-point storage
+// mass, unchanged to the bit (i16_conserve_bits), which floating-point storage
 // cannot.  Rounding is to nearest even through the 1.5 * 2^23 magic
 // constant (x + 1.5 * 2^23 rounds x to an integer for |x| < 2^22); values
 // outside the range saturate.
@@ -207,17 +207,22 @@ struct Storage<LBM_STORE_I16S> {
 // for the fixed-point storage: populations 1..8 round to their nearest
 // step, and population 0 takes the rest of the node's pre-collision mass
 // d (a sum of stored values, exact), so the stored sum equals d exactly.
-// h: shifted post-collision values; on return, multiples of Q.
-__device__ __forceinline__ void i16_conserve(float (&h)[9], float d) {
-  float s = 0.0f;
+// h: shifted post-collision values.  b[k]: the int16 bits of the stored
+// step counts in the low half of each word.  The rounding yields
+// t = n + 1.5 * 2^23 as a float, whose bit pattern is that of 1.5 * 2^23
+// plus n, so the step counts add up as integers without a conversion.
+__device__ __forceinline__ void i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9]) {
+  const unsigned mb = __float_as_uint(I16_MAGIC);
+  unsigned s = 0u;  // sum of the steps of populations 1..8 (two's complement)
 #pragma unroll
   for (int k = 1; k < 9; ++k) {
-    const float n = i16_steps(h[k]);
-    s += n;  // exact: integers below 2^24
-    h[k] = n * I16_Q;
+    const float t = fminf(fmaxf(fmaf(h[k], I16_IQ, I16_MAGIC), I16_MAGIC - 32768.0f), I16_MAGIC + 32767.0f);
+    b[k] = __float_as_uint(t);
+    s += b[k] - mb;
   }
-  const float n0 = fminf(fmaxf(fmaf(d, I16_IQ, -s), -32768.0f), 32767.0f);
-  h[0] = n0 * I16_Q;
+  // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is exact
+  const int n0 = (int)(__float_as_uint(fmaf(d, I16_IQ, I16_MAGIC)) - mb) - (int)s;
+  b[0] = (unsigned)min(max(n0, -32768), 32767);
 }
 
 // The general (unshifted) path holds f = n Q + w rounded to FP32; the nearest
@@ -236,9 +241,10 @@ __device__ __forceinline__ void i16_store_node(const float (&f)[9], const float 
   float h[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) h[k] = f[k] - w[k];
-  i16_conserve(h, mass);
+  unsigned b[9];
+  i16_conserve_bits(h, mass, b);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) out[k] = (short)i16_bits(h[k] * I16_IQ);
+  for (int k = 0; k < 9; ++k) out[k] = (short)(b[k] & 0xffffu);
 }
 
 template <int BYTES>

@@ -462,6 +462,27 @@ __device__ __forceinline__ float node_sum(const float (&h)[9]) {
   return ((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7])) + h[8];
 }
 
+// Fixed-point storage: quantise V nodes' post-collision values h with each
+// node's pre-collision mass kept (i16_conserve_bits) and store the nine
+// planes from p (population k at p + k * plane), two step counts per word.
+template <int V>
+__device__ __forceinline__ void store_i16_conserved(short* p, size_t plane, const float (&h)[V][9],
+                                                    const float (&mass)[V]) {
+  unsigned b[V][9];
+#pragma unroll
+  for (int i = 0; i < V; ++i) i16_conserve_bits(h[i], mass[i], b[i]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    short raw[V];
+#pragma unroll
+    for (int i = 0; i < V; i += 2) {
+      const unsigned w = __byte_perm(b[i][k], b[i + 1][k], 0x5410);
+      memcpy(&raw[i], &w, sizeof(w));
+    }
+    store_vec<short, V>(p + (size_t)k * plane, raw);
+  }
+}
+
 // Moments, collision and stores of one lane's V nodes (x0.., row y) of a
 // plain segment, from the gathered stored values h.
 template <class P, int MODEL, bool PL, int ST, int V, int FORCE>
@@ -487,11 +508,14 @@ __device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9],
   for (int i = 0; i < V; ++i) {
     const float st = collide_lean<P, MODEL, PL, FORCE>(p, h[i], PL ? tau[i] : 0.0f);
     if (PL) tau[i] = st;
-    if constexpr (ST == LBM_STORE_I16S) i16_conserve(h[i], mass[i]);
   }
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
+  if constexpr (ST == LBM_STORE_I16S) {
+    store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     float c[V];

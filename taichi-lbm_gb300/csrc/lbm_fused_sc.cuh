@@ -215,11 +215,7 @@ __device__ __forceinline__ void sc_stage_collide(const P& p, const unsigned char
     for (int i = 0; i < V; ++i) h[i][k] = c[i];
   }
 #pragma unroll
-  for (int i = 0; i < V; ++i) {
-    const float mass = ST == LBM_STORE_I16S ? node_sum(h[i]) : 0.0f;
-    collide_lean<P, MODEL, false, 2>(p, h[i], 0.0f, Fx[i], Fy[i]);
-    if constexpr (ST == LBM_STORE_I16S) i16_conserve(h[i], mass);
-  }
+  for (int i = 0; i < V; ++i) collide_lean<P, MODEL, false, 2>(p, h[i], 0.0f, Fx[i], Fy[i]);
   if (x0 >= p.nx) return;
   T* dst = reinterpret_cast<T*>(p.dst);
   const size_t rowoff = (size_t)y * p.pitch;

@@ -16,6 +16,7 @@ collision runs through the per-stage kernels, then n-1 fused launches (each
 and boundary pass and the moment kernels.
 """
 import ctypes
+import warnings
 import zlib
 
 import numpy as np
@@ -315,6 +316,13 @@ class FusedSolver:
                 A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
                 lb._f, lb._f2 = lb._f2, lb._f
         else:
+            if self.storage == A.STORE_I16S:
+                # the fixed-point steps saturate at +-2^15 (|f - w rho_ref| >= 1/16)
+                st = self.fbuf[par.value]
+                self.saturated = int(torch.count_nonzero((st == 32767) | (st == -32768)).item())
+                if self.saturated:
+                    warnings.warn(f"fixed-point storage saturated at {self.saturated} stored values "
+                                  "(|f - w rho_ref| >= 1/16); use fp32 or fp16s for this flow")
             A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
             A.call("lbm_plan_export", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
         if self.powerlaw:
