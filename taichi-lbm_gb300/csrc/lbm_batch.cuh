@@ -63,18 +63,18 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLatt
 }
 
 // Marked lanes (bounce-back links, boundary programs, saved moments,
-// inactive nodes) of every lattice in the table, one thread per lane entry
-// ((y * nseg + seg) * 32 + lane): the general per-node path.
+// inactive nodes) of every lattice in the table, V threads per lane entry
+// ((y * nseg + seg) * 32 + lane), one per node: the general per-node path.
 template <int MODEL, bool PL, int ST, int V>
 __global__ void __launch_bounds__(128) k_batch_lanes(const BatchLattice* __restrict__ lats,
                                                      const BatchTile* __restrict__ tiles, int ntiles, int sp) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ntiles) return;
-  const BatchTile tile = tiles[t];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ntiles * V) return;
+  const BatchTile tile = tiles[t / V];
   const FusedParams& p = lats[tile.lat].full[view_of(lats, tile.lat, sp)];
   const int item = tile.item >> 5, lane = tile.item & 31;
   const int y = item / p.nseg;
-  lane_general<MODEL, PL, ST, V>(p, y, (item - y * p.nseg) * 32 * V + lane * V);
+  lane_node<MODEL, PL, ST>(p, y, (item - y * p.nseg) * 32 * V + lane * V + (int)(t % V));
 }
 
 // Shan-Chen strips (item = chunk * nseg + seg) of every lattice in the
@@ -185,7 +185,7 @@ int launch_batch_seg(BatchGroup& g, const BatchLattice* lats, const BatchTile* t
   if (g.count == 0) return LBM_OK;
   const BatchTile* t = tiles + g.offset;
   if (g.kind == BATCH_SPECIAL) {
-    k_batch_lanes<MODEL, PL, ST, V><<<(unsigned)((g.count + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
+    k_batch_lanes<MODEL, PL, ST, V><<<(unsigned)(((long long)g.count * V + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
     return lbm_err::launch("batched step (marked lanes)");
   }
   auto kern = g.force ? k_batch_lean<MODEL, PL, ST, V, 1> : k_batch_lean<MODEL, PL, ST, V, 0>;

@@ -675,27 +675,26 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   }
 }
 
-// The general step of one lane's V nodes (x0.., row y) from per-node
-// gathers: what fused_tail does for a whole segment, for a lane the lane
-// mask marks.  A node outside the collision group keeps its stored values
-// (copied bit for bit).
-template <int MODEL, bool PL, int ST, int V>
-__device__ __forceinline__ void lane_general(const FusedParams& p, int y, int x0) {
+// The general step of one node (x, row y) of a lane the lane mask marks,
+// from per-node gathers: what fused_tail does for a whole segment.  A node
+// outside the collision group keeps its stored values (copied bit for bit).
+// One thread per node: the path is a chain of dependent loads (node code,
+// gathers, boundary reads), so nodes of a lane run side by side, not in turn.
+template <int MODEL, bool PL, int ST>
+__device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
   using S = Storage<ST>;
   using T = typename S::T;
   const T* src = reinterpret_cast<const T*>(p.src);
   T* dst = reinterpret_cast<T*>(p.dst);
   const float Fx = p.has_force ? p.gx : 0.0f, Fy = p.has_force ? p.gy : 0.0f;
-#pragma unroll 1
-  for (int i = 0; i < V; ++i) {
-    const int x = x0 + i;
-    if (x >= p.nx) break;
+  if (x >= p.nx) return;
+  {
     const size_t q = (size_t)y * p.pitch + x;
     const unsigned code = p.code[q];
     if (!(code & LBM_CODE_ACTIVE)) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = load1(src + (size_t)k * p.plane + q);
-      continue;
+      return;
     }
     float f[9];
     gather_node<ST>(p, x, y, f);
@@ -730,15 +729,15 @@ __device__ __forceinline__ void lane_general(const FusedParams& p, int y, int x0
   }
 }
 
-// One thread per listed lane.
+// V threads per listed lane, one per node.
 template <int MODEL, bool PL, int ST, int V>
 __global__ void __launch_bounds__(128) k_fused_lanes(const FusedParams p) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.nlanes) return;
-  const int e = p.lanes[t];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)p.nlanes * V) return;
+  const int e = p.lanes[t / V];
   const int item = e >> 5, lane = e & 31;
   const int y = item / p.nseg;
-  lane_general<MODEL, PL, ST, V>(p, y, (item - y * p.nseg) * 32 * V + lane * V);
+  lane_node<MODEL, PL, ST>(p, y, (item - y * p.nseg) * 32 * V + lane * V + (int)(t % V));
 }
 
 // Stream + boundary pass only (the last half step of a fused run): writes the

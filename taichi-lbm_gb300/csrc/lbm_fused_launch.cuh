@@ -150,7 +150,7 @@ template <int MODEL, bool PL, int ST, int V>
 int launch_two_pass(const FusedParams& p, unsigned blocks, cudaStream_t s, cudaStream_t s2) {
   if (p.lane_mask) {  // lane-granular form: the marked lanes, then every segment
     if (p.nlanes > 0) {
-      k_fused_lanes<MODEL, PL, ST, V><<<(unsigned)((p.nlanes + 127) / 128), 128, 0, s2>>>(p);
+      k_fused_lanes<MODEL, PL, ST, V><<<(unsigned)(((long long)p.nlanes * V + 127) / 128), 128, 0, s2>>>(p);
       int rc = lbm_err::launch("fused step (marked lanes)");
       if (rc) return rc;
     }

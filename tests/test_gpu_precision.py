@@ -69,7 +69,15 @@ def test_power_law_contraction_vs_fp64(tl, oracle_refs, n, storage):
     from taichi_lbm.workloads import contraction_channel
     nx, ny, h, steps = SIZE
     lb, me, coll, be = contraction_channel(tl, nx, ny, h, n=n)
-    tl.FusedSolver(lb, me, coll, be, storage=storage).step(steps)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage)
+    if storage == "i16s" and n == 0.5:
+        # the unsteady shear-thinning jet reaches |f - w rho_ref| = 0.13,
+        # beyond the fixed-point range (1/16): finish() must report it
+        with pytest.warns(UserWarning, match="saturated"):
+            solver.step(steps)
+        assert solver.saturated > 0
+        return
+    solver.step(steps)
     got = fields_of(lb)
     ref64, ref32 = oracle_refs[n]
     err = {k: rel_err(got[k], ref64[k]) for k in ("rho", "vel")}
