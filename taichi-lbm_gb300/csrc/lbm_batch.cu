@@ -300,8 +300,10 @@ int rebuild(LbmBatch* b) {
     } else {
       // every segment on the plain path (fully marked ones skipped), marked lanes one by one
       const std::vector<uint32_t>& masks = m.masks;
-      auto& tl = bucket({lbm::BATCH_LEAN, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, p.has_force});
-      auto& ts = bucket({lbm::BATCH_SPECIAL, pl->d.model, pw, pl->d.storage, pl->d.nodes_per_thread, 0});
+      // lean groups hold every collision model (the kernel branches per lattice);
+      // the marked-lane group also every fluid model
+      auto& tl = bucket({lbm::BATCH_LEAN, -1, pw, pl->d.storage, pl->d.nodes_per_thread, p.has_force});
+      auto& ts = bucket({lbm::BATCH_SPECIAL, -1, -1, pl->d.storage, pl->d.nodes_per_thread, 0});
       for (int item = 0; item < (int)masks.size(); ++item) {
         const uint32_t mk = masks[item];
         if (mk != 0xffffffffu) tl.push_back({lat, item});

@@ -37,8 +37,11 @@ constexpr int BATCH_WARPS = 8;  // warps per block of the segment kinds
 // hardware balances the blocks, so work that runs beside this kernel on
 // other streams never leaves a statically assigned share behind).  Every
 // lattice's tiles are padded to whole blocks (item -1), so a block serves one
-// lattice and stages its parameters in shared memory once.
-template <int MODEL, bool PL, int ST, int V, int FORCE>
+// lattice and stages its parameters in shared memory once.  The collision
+// model is the lattice's (a branch uniform over the block), so lattices of
+// every model share one launch; each branch is the single-lattice kernel's
+// own collision and store, so results stay bit-identical to it.
+template <bool PL, int ST, int V, int FORCE>
 __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLattice* __restrict__ lats,
                                                                   const BatchTile* __restrict__ tiles, int ntiles,
                                                                   int sp) {
@@ -59,13 +62,17 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLatt
   if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
   else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
   if (mask == 0xffffffffu) return;
-  lean_collide_store<LeanParams, MODEL, PL, ST, V, FORCE>(p, h, y, x0, (mask >> lane) & 1u);
+  const bool skip = (mask >> lane) & 1u;
+  if (p.model == LBM_BGK) lean_collide_store<LeanParams, LBM_BGK, PL, ST, V, FORCE>(p, h, y, x0, skip);
+  else if (p.model == LBM_TRT) lean_collide_store<LeanParams, LBM_TRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+  else lean_collide_store<LeanParams, LBM_MRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
 }
 
 // Marked lanes (bounce-back links, boundary programs, saved moments,
 // inactive nodes) of every lattice in the table, V threads per lane entry
-// ((y * nseg + seg) * 32 + lane), one per node: the general per-node path.
-template <int MODEL, bool PL, int ST, int V>
+// ((y * nseg + seg) * 32 + lane), one per node: the general per-node path,
+// for the lattice's collision model and fluid model.
+template <int ST, int V>
 __global__ void __launch_bounds__(128) k_batch_lanes(const BatchLattice* __restrict__ lats,
                                                      const BatchTile* __restrict__ tiles, int ntiles, int sp) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,7 +81,15 @@ __global__ void __launch_bounds__(128) k_batch_lanes(const BatchLattice* __restr
   const FusedParams& p = lats[tile.lat].full[view_of(lats, tile.lat, sp)];
   const int item = tile.item >> 5, lane = tile.item & 31;
   const int y = item / p.nseg;
-  lane_node<MODEL, PL, ST>(p, y, (item - y * p.nseg) * 32 * V + lane * V + (int)(t % V));
+  const int x = (item - y * p.nseg) * 32 * V + lane * V + (int)(t % V);
+  switch (p.model * 2 + (p.fluid_model == LBM_POWERLAW ? 1 : 0)) {
+    case 0: lane_node<LBM_BGK, false, ST>(p, y, x); break;
+    case 1: lane_node<LBM_BGK, true, ST>(p, y, x); break;
+    case 2: lane_node<LBM_TRT, false, ST>(p, y, x); break;
+    case 3: lane_node<LBM_TRT, true, ST>(p, y, x); break;
+    case 4: lane_node<LBM_MRT, false, ST>(p, y, x); break;
+    default: lane_node<LBM_MRT, true, ST>(p, y, x); break;
+  }
 }
 
 // Shan-Chen strips (item = chunk * nseg + seg) of every lattice in the
@@ -180,30 +195,20 @@ int batch_grid(K kern, int threads, int tiles_per_block, int count, int* blocks)
   return need < *blocks ? need : *blocks;
 }
 
-template <int MODEL, bool PL, int ST, int V>
-int launch_batch_seg(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
+// groups of the segment kinds: lean groups per (power law, force), every
+// collision model in one launch; one marked-lane group for every model
+template <int ST, int V>
+int launch_batch_v(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
   if (g.count == 0) return LBM_OK;
   const BatchTile* t = tiles + g.offset;
   if (g.kind == BATCH_SPECIAL) {
-    k_batch_lanes<MODEL, PL, ST, V><<<(unsigned)(((long long)g.count * V + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
+    k_batch_lanes<ST, V><<<(unsigned)(((long long)g.count * V + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
     return lbm_err::launch("batched step (marked lanes)");
   }
-  auto kern = g.force ? k_batch_lean<MODEL, PL, ST, V, 1> : k_batch_lean<MODEL, PL, ST, V, 0>;
+  auto kern = g.powerlaw ? (g.force ? k_batch_lean<true, ST, V, 1> : k_batch_lean<true, ST, V, 0>)
+                         : (g.force ? k_batch_lean<false, ST, V, 1> : k_batch_lean<false, ST, V, 0>);
   kern<<<(unsigned)((g.count + BATCH_WARPS - 1) / BATCH_WARPS), BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
   return lbm_err::launch("batched step (plain segments)");
-}
-
-template <int ST, int V>
-int launch_batch_v(BatchGroup& g, const BatchLattice* lats, const BatchTile* tiles, int sp, cudaStream_t s) {
-  switch (g.model * 2 + (g.powerlaw ? 1 : 0)) {
-    case 0: return launch_batch_seg<LBM_BGK, false, ST, V>(g, lats, tiles, sp, s);
-    case 1: return launch_batch_seg<LBM_BGK, true, ST, V>(g, lats, tiles, sp, s);
-    case 2: return launch_batch_seg<LBM_TRT, false, ST, V>(g, lats, tiles, sp, s);
-    case 3: return launch_batch_seg<LBM_TRT, true, ST, V>(g, lats, tiles, sp, s);
-    case 4: return launch_batch_seg<LBM_MRT, false, ST, V>(g, lats, tiles, sp, s);
-    case 5: return launch_batch_seg<LBM_MRT, true, ST, V>(g, lats, tiles, sp, s);
-    default: return lbm_err::set(LBM_ERR_ARG, "batch: collision model %d", g.model);
-  }
 }
 
 template <int ST>

@@ -88,6 +88,7 @@ struct LeanParams {
   float g_coh, sc_T;
   LbmEos eos;
   int sc_rows;  // rows of a strip item
+  int model;    // collision model (batched kernels branch on it per lattice)
   const uint32_t* lane_mask;  // lanes not to store (FusedParams::lane_mask), or null
 };
 
@@ -136,6 +137,7 @@ inline LeanParams lean_of(const FusedParams& f) {
   l.sc_T = f.sc_T;
   l.eos = f.eos;
   l.sc_rows = 16;
+  l.model = f.model;
   l.lane_mask = f.lane_mask;
   return l;
 }
