@@ -310,7 +310,7 @@ int rebuild(LbmBatch* b) {
         for (int l = 0; l < 32; ++l)
           if (mk >> l & 1u) ts.push_back({lat, item * 32 + l});
       }
-      while (tl.size() % lbm::BATCH_WARPS) tl.push_back({lat, -1});  // whole blocks per lattice
+      while (tl.size() % (lbm::BATCH_WARPS * lbm::BATCH_TPW)) tl.push_back({lat, -1});  // whole blocks per lattice
     }
     if (m.monitored) {
       BatchMonitor bm;

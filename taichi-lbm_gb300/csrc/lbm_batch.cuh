@@ -32,10 +32,15 @@ struct BatchTile {
 __device__ __forceinline__ int view_of(const BatchLattice* lats, int lat, int sp) { return (sp ^ lats[lat].flip) & 1; }
 
 constexpr int BATCH_WARPS = 8;  // warps per block of the segment kinds
+// tiles per warp of the lean kind: a block stages its lattice's parameters
+// once for BATCH_WARPS * BATCH_TPW tiles, so the two dependent loads in
+// front of the first tile (tile -> lattice -> parameters) are paid once
+constexpr int BATCH_TPW = 2;
 
-// Plain-path segments of every lattice in the table: one warp per tile (the
-// hardware balances the blocks, so work that runs beside this kernel on
-// other streams never leaves a statically assigned share behind).  Every
+// Plain-path segments of every lattice in the table: BATCH_TPW tiles per
+// warp, not persistent (the hardware balances the blocks, so work that runs
+// beside this kernel on other streams never leaves a statically assigned
+// share behind).  Every
 // lattice's tiles are padded to whole blocks (item -1), so a block serves one
 // lattice and stages its parameters in shared memory once.  The collision
 // model is the lattice's (a branch uniform over the block), so lattices of
@@ -47,25 +52,28 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLatt
                                                                   int sp) {
   __shared__ LeanParams p;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t0 = blockIdx.x * BATCH_WARPS;
+  const int t0 = blockIdx.x * (BATCH_WARPS * BATCH_TPW);
   const int lat = tiles[t0].lat;
   copy_words(&p, &lats[lat].lean[view_of(lats, lat, sp)], threadIdx.x, BATCH_WARPS * 32);
   __syncthreads();
-  const BatchTile tile = tiles[t0 + warp];
-  if (tile.item < 0) return;
-  const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
-  const int seg = tile.item - y * p.nseg;
-  const int x0s = seg * 32 * V, x0 = x0s + lane * V;
-  uint32_t mask;  // lanes k_batch_lanes stores
-  ldg_early(p.lane_mask + tile.item, mask);
-  float h[V][9];
-  if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
-  else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
-  if (mask == 0xffffffffu) return;
-  const bool skip = (mask >> lane) & 1u;
-  if (p.model == LBM_BGK) lean_collide_store<LeanParams, LBM_BGK, PL, ST, V, FORCE>(p, h, y, x0, skip);
-  else if (p.model == LBM_TRT) lean_collide_store<LeanParams, LBM_TRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
-  else lean_collide_store<LeanParams, LBM_MRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+#pragma unroll 1
+  for (int j = 0; j < BATCH_TPW; ++j) {  // consecutive warps take consecutive tiles
+    const BatchTile tile = tiles[t0 + j * BATCH_WARPS + warp];
+    if (tile.item < 0) continue;
+    const int y = fast_div(tile.item, p.nseg_mul, p.nseg_shift);
+    const int seg = tile.item - y * p.nseg;
+    const int x0s = seg * 32 * V, x0 = x0s + lane * V;
+    uint32_t mask;  // lanes k_batch_lanes stores
+    ldg_early(p.lane_mask + tile.item, mask);
+    float h[V][9];
+    if (x0s > 0 && x0s + 32 * V < p.nx) gather_interior<LeanParams, ST, V>(p, y, x0, lane, h);
+    else gather_edge<LeanParams, ST, V>(p, y, x0, lane, h);
+    if (mask == 0xffffffffu) continue;
+    const bool skip = (mask >> lane) & 1u;
+    if (p.model == LBM_BGK) lean_collide_store<LeanParams, LBM_BGK, PL, ST, V, FORCE>(p, h, y, x0, skip);
+    else if (p.model == LBM_TRT) lean_collide_store<LeanParams, LBM_TRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+    else lean_collide_store<LeanParams, LBM_MRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+  }
 }
 
 // Marked lanes (bounce-back links, boundary programs, saved moments,
@@ -207,7 +215,8 @@ int launch_batch_v(BatchGroup& g, const BatchLattice* lats, const BatchTile* til
   }
   auto kern = g.powerlaw ? (g.force ? k_batch_lean<true, ST, V, 1> : k_batch_lean<true, ST, V, 0>)
                          : (g.force ? k_batch_lean<false, ST, V, 1> : k_batch_lean<false, ST, V, 0>);
-  kern<<<(unsigned)((g.count + BATCH_WARPS - 1) / BATCH_WARPS), BATCH_WARPS * 32, 0, s>>>(lats, t, g.count, sp);
+  kern<<<(unsigned)((g.count + BATCH_WARPS * BATCH_TPW - 1) / (BATCH_WARPS * BATCH_TPW)), BATCH_WARPS * 32, 0, s>>>(
+      lats, t, g.count, sp);
   return lbm_err::launch("batched step (plain segments)");
 }
 
