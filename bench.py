@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched Shan-Chen lines")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--requests", type=int, default=64, help="requests in the served stream")
+    ap.add_argument("--mix-only", type=int, default=0, metavar="N",
+                    help="only time the batched step of the first N served requests (fp16s, all packed)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -531,10 +533,41 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def run_mix(a):
+    """The batched step of a served mix on its own: the first N requests of
+    the seeded served stream (fp16s), all in the packed tile table, direct
+    launches (no graph), K timed steps after W warm-up steps."""
+    import torch
+    import taichi_lbm as tl
+    from taichi_lbm.serving import request_stream
+    reqs = request_stream(a.mix_only, 20.0)
+    solvers = [r.build(tl) for r in reqs]
+    nodes = sum(s.coll.group.n for s in solvers)
+    batch = tl.Batch(graphs=False, solo_nodes=0)
+    for s in solvers:
+        batch.add(s)
+    batch.run(a.warmup)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    batch.run(a.steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    print(json.dumps({"metric": METRIC, "value": round(nodes / ms / 1e3, 1), "unit": METRIC, "steps": a.steps,
+                      "warmup": a.warmup, "ms_per_step": round(ms, 4), "nodes": nodes, "info": batch.info(),
+                      "config": {"workload": f"batched step of the first {a.mix_only} served requests (seed "
+                                             "20261203), fp16s, every member packed, direct launches"}}))
+    batch.close()
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.mix_only:
+        run_mix(a)
     else:
         run_ours(a)
 
