@@ -169,11 +169,12 @@ def dist_setup():
     return 0, 1, 0, None
 
 
-def max_over_ranks(v, dist):
+def max_over_ranks(v, dist, device="cuda"):
+    """The slowest rank's value (replicas are timed by the slowest)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
