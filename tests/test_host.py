@@ -199,3 +199,43 @@ def test_segment_flags_mark_only_special_segments():
                                              BoundaryItem(A.BC_PERIODIC, nodes, name="p")], 4)
     assert cp.seg_flags.shape == (ny, 3) and cp.seg_flags.sum() == 0
     assert (cp.code == A.CODE_ACTIVE).all()
+
+
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_lane_mask_and_lane_list_cover_exactly_the_special_nodes(V):
+    """Bit l of lane_mask[y, seg] is set exactly when one of lane l's V nodes is
+    not plain (bounce-back link, boundary program, saved moments, outside the
+    collision group); the lane list holds the set bits as (y * nseg + seg) * 32
+    + l; a segment's flag is nonzero exactly when some bit of its mask is set.
+    389 columns leave a partial last segment at every V."""
+    from taichi_lbm import _capi as A
+    from taichi_lbm._plan import BoundaryItem, compile_plan
+    nx, ny = 389, 12
+    mask = np.ones((nx, ny), np.int32)
+    mask[100:110, 4:8] = -1  # a solid block
+    links = links_from_mask(mask)
+    fluid = np.argwhere(mask == 1).astype(np.int32)
+    c = [(0, 0), (1, 0), (0, 1), (-1, 0), (0, -1), (1, 1), (-1, 1), (-1, -1), (1, -1)]
+    missing = np.zeros((nx, ny), bool)
+    for k in range(1, 9):
+        cx, cy = c[k]
+        src = np.pad(mask == 1, 1, constant_values=False)[1 - cx:1 - cx + nx, 1 - cy:1 - cy + ny]
+        missing |= ~src
+    wall = np.argwhere((mask == 1) & missing).astype(np.int32)
+    cp = compile_plan(nx, ny, fluid, links, [BoundaryItem(A.BC_FLUID, fluid, name="f"),
+                                             BoundaryItem(A.BC_PERIODIC, fluid, name="p"),
+                                             BoundaryItem(A.BC_BOUNCEBACK, wall, name="w")], V)
+    nseg = -(-nx // (32 * V))
+    lm = np.asarray(cp.lane_mask, np.uint32).reshape(ny, nseg)
+    plain = cp.code == A.CODE_ACTIVE  # (nx, ny)
+    want = np.zeros((ny, nseg), np.uint64)
+    for y in range(ny):
+        for x in range(nx):
+            if not plain[x, y]:
+                seg, lane = divmod(x // V, 32)
+                want[y, seg] |= np.uint64(1) << np.uint64(lane)
+    assert np.array_equal(lm.astype(np.uint64), want)
+    ys, segs = np.nonzero(lm)
+    expect = [((y * nseg + s) * 32 + l) for y, s in zip(ys, segs) for l in range(32) if (lm[y, s] >> l) & 1]
+    assert sorted(np.asarray(cp.lanes).tolist()) == sorted(expect)
+    assert np.array_equal(np.asarray(cp.seg_flags).reshape(ny, nseg) != 0, lm != 0)
