@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--requests", type=int, default=64, help="requests in the served stream")
     ap.add_argument("--mix-only", type=int, default=0, metavar="N",
                     help="only time the batched step of the first N served requests (fp16s, all packed)")
+    ap.add_argument("--mix-v", type=int, default=None, help="nodes per thread of the --mix-only members")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -542,7 +543,7 @@ def run_mix(a):
     import taichi_lbm as tl
     from taichi_lbm.serving import request_stream
     reqs = request_stream(a.mix_only, 20.0)
-    solvers = [r.build(tl) for r in reqs]
+    solvers = [r.build(tl, nodes_per_thread=a.mix_v) for r in reqs]
     nodes = sum(s.coll.group.n for s in solvers)
     batch = tl.Batch(graphs=False, solo_nodes=0)
     for s in solvers:
@@ -559,7 +560,8 @@ def run_mix(a):
     print(json.dumps({"metric": METRIC, "value": round(nodes / ms / 1e3, 1), "unit": METRIC, "steps": a.steps,
                       "warmup": a.warmup, "ms_per_step": round(ms, 4), "nodes": nodes, "info": batch.info(),
                       "config": {"workload": f"batched step of the first {a.mix_only} served requests (seed "
-                                             "20261203), fp16s, every member packed, direct launches"}}))
+                                             "20261203), fp16s, every member packed, direct launches",
+                                 "nodes_per_thread": solvers[0].V}}))
     batch.close()
 
 
