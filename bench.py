@@ -314,17 +314,12 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
     mean_work = sum(r.nodes * r.steps for r in probe) / n
     rate = 0.8 * capacity_mlups * 1e6 / mean_work
     reqs = request_stream(n, rate, storage=storage)
-    # autotune (before the stream starts): nodes per thread per model at three
-    # lattice sizes, and the batch's solo threshold on a sample of the stream
+    # autotune (before the stream starts) in the batch itself, on the first 16
+    # requests: the members' nodes per thread and the solo threshold (a
+    # lattice's fastest V alone is not its fastest in a packed mix)
     t0 = time.perf_counter()
     tuner = tl.Autotuner(steps=30, warmup=5)
-    from taichi_lbm.serving import Request
-    for model in ("bgk", "trt", "mrt"):
-        for nx in (256, 1024, 2048):
-            r = Request(0, nx, nx // 4, model, 0.55, 100, storage=storage)
-            tuner.nodes_per_thread(r.tune_key(), storage, lambda V, r=r: r.build(tl, nodes_per_thread=V))
-    tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=tuner.lookup(r.tune_key(), "V"))
-                                           for r in reqs[:16]], storage, tune_v=False)
+    tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=V) for r in reqs[:16]], storage)
     tune_s = time.perf_counter() - t0
     torch.cuda.empty_cache()
     srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=200, builders=4, autotuner=tuner)
@@ -354,9 +349,8 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
                                 "drag/lift, one after another",
                 "clocks": clk.summary(),
                 "autotune": {"seconds": round(tune_s, 1), "table": tuner.table,
-                             "what": "nodes per thread per model at 256/1024/2048 x NX/4 (nearest size bucket "
-                                     "used per request) and the batch's solo threshold on the first 16 "
-                                     "requests, each candidate timed with CUDA events over 30 steps"}})
+                             "what": "nodes per thread and solo threshold of the batch, tuned on the first 16 "
+                                     "requests, each candidate timed with CUDA events over 30 batched steps"}})
     out["vs_alone_fp32"] = round(out["MLUPS"] / out["alone_fp32_MLUPS"], 3)
     return out
 

@@ -90,11 +90,13 @@ class Server:
 
     def __init__(self, tl, hbm_budget, graphs=True, slice_steps=200, keep_fields=False, builders=1, ahead=2,
                  reserve_bytes=16 << 30, autotuner=None, batch_key="served"):
-        """autotuner: an Autotuner whose table gives each request's nodes per
-        thread (by Request.tune_key) and the batch's shape (entry
-        `batch_key`); shapes it has no entry for keep the defaults."""
+        """autotuner: an Autotuner whose table gives the batch's shape (entry
+        `batch_key`: solo threshold and, when tuned in the batch, the nodes per
+        thread of every member) or else each request's nodes per thread (by
+        Request.tune_key); shapes it has no entry for keep the defaults."""
         self.tl = tl
         self.autotuner = autotuner
+        self.batch_key = batch_key
         self.batch = Batch(graphs=graphs, **(autotuner.batch_kwargs(batch_key) if autotuner else {}))
         self.budget = int(hbm_budget)
         self.used = 0
@@ -116,7 +118,11 @@ class Server:
     def _build(self, req, stream):
         """Builder thread: lattice, plan, first step and first drag/lift row
         on `stream`; returns what the scheduler needs to join the batch."""
-        V = self.autotuner.lookup(req.tune_key(), "V") if self.autotuner else None
+        V = None
+        if self.autotuner:
+            V = self.autotuner.table.get(self.batch_key, {}).get("V")
+            if V is None:
+                V = self.autotuner.lookup(req.tune_key(), "V")
         with torch.cuda.stream(stream):
             solver = req.build(self.tl, nodes_per_thread=V)
             mon = Batch.prepare(solver, req.steps)
