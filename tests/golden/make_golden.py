@@ -306,6 +306,58 @@ def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bg
     return lb, me, coll, be, lb.sc_field, bsc
 
 
+def build_shanchen_mc(ti, tl, case, nx, ny, *, g_coh, rho_init, nu, rho0, T=1.0, gravity=None):
+    """Fully periodic multi-component Shan-Chen lattice (ShanChenForceC2,
+    SC_psi per component, BGK per component with the mixture velocity): every
+    node is fluid, so fluid_strategy is true everywhere and no adhesion acts."""
+    nc = len(nu)
+    lb = tl.LBField(case.meta["name"], nx, ny, nc)
+    if gravity is not None:
+        lb.set_gravity(ti.Vector(list(gravity)))
+        case.meta["gravity"] = list(gravity)
+    be = tl.BoundaryEngine()
+    cls = tl.BoundaryClassifier(ti.field(float, shape=(nx, ny)))
+
+    @ti.func
+    def fluid_fn(i, j):
+        return lb.mask[i, j] == 1
+    fluid = tl.FluidBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    fluid.precompute(classifier=cls)
+    be.add_boundary_condition("fluid", fluid)
+    case.bc("fluid", "fluid", group_nodes(fluid.group))
+    per = tl.PeriodicAllBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    per.precompute(classifier=cls)
+    be.add_boundary_condition("stream", per)
+    case.bc("stream", "periodic", group_nodes(per.group))
+    lb.neighbor_classify()
+    me = tl.MacroscopicEngine(fluid.group)
+    params = {"group": fluid.group, "fluid_model": tl.NewtonianFluid(nu[0]), "NX": nx, "NY": ny,
+              "num_components": nc, "shearviscosity": list(nu)}
+    coll = tl.BGKCollision(params)
+    case.meta["collision"] = {"model": "bgk", "nu": list(nu)}
+
+    @ti.func
+    def everywhere(i, j):
+        return True
+    psis = [tl.SC_psi(rho0=r) for r in rho0]
+    g = ti.Matrix([list(row) for row in g_coh])
+    lb.sc_field = tl.ShanChenForceC2({"lb_field": lb, "g_coh": g, "gadh": [0.0] * nc, "group": fluid.group,
+                                      "psi_list": psis, "fluid_strategy": everywhere})
+    case.meta["sc"] = {"g_coh": [list(row) for row in g_coh], "psi": [["sc", r] for r in rho0],
+                       "components": nc}
+    bsc = tl.BoundaryEngineSC()
+    bsc.add_boundary_condition("periodicLR", tl.PeriodicPsi_LR())
+    bsc.add_boundary_condition("periodicBT", tl.PeriodicPsi_BT())
+    case.meta["psi_bcs"] = ["periodic_lr", "periodic_bt"]
+    lb.T.fill(T)
+    case.meta["T"] = T
+    for (i, j) in group_nodes(fluid.group):
+        for c in range(nc):
+            lb.rho[i, j, c] = rho_init[c][i, j]
+    lb.init_LBM(coll, fluid.group)
+    return lb, me, coll, be, lb.sc_field, bsc
+
+
 def step_fn(lb, me, coll, be, sc, bsc, kind):
     def standard():
         me.density(lb)
@@ -430,6 +482,17 @@ def case_table():
                                             g_coh=-1.0, rho_init=rho_vdw,
                                             collision=("trt", {"magic": [0.25]}), nu=0.1,
                                             T=0.85 * 4.0 / 7.0), "shanchen", 30, "f64", (16, 16))
+    # two components: a disc of component 0 in component 1, seeded noise
+    mx, my = 24, 20
+    ii, jj = np.meshgrid(np.arange(mx), np.arange(my), indexing="ij")
+    disc = ((ii - 11.5) ** 2 + (jj - 9.5) ** 2) < 36.0
+    a = np.where(disc, 1.0, 0.06) * (1.0 + rng.uniform(-0.01, 0.01, size=(mx, my)))
+    b = np.where(disc, 0.06, 1.0) * (1.0 + rng.uniform(-0.01, 0.01, size=(mx, my)))
+    for fp in ("f32", "f64"):
+        t[f"mc_sc2_bgk_{fp}"] = ("shanchen_mc", dict(g_coh=((0.0, 0.9), (0.9, 0.0)), rho_init=(a, b),
+                                                    nu=(1.0 / 6.0, 0.1), rho0=(1.0, 1.0),
+                                                    gravity=(0.0, -1e-5) if fp == "f32" else None),
+                                 "shanchen", 30, fp, (mx, my))
     return t
 
 
@@ -444,8 +507,11 @@ def run_case(ref_root, name, spec, out_dir):
         warnings.simplefilter("ignore")
         if builder == "channel":
             lb, me, coll, be, sc, bsc = build_channel(ti, tl, case, nx, ny, **kw)
+        elif builder == "shanchen_mc":
+            lb, me, coll, be, sc, bsc = build_shanchen_mc(ti, tl, case, nx, ny, **kw)
         else:
             lb, me, coll, be, sc, bsc = build_shanchen(ti, tl, case, nx, ny, **kw)
+        init_rho_all = lb.rho.to_numpy().copy()
         init_rho = lb.rho.to_numpy()[:, :, 0].copy()
         init_vel = lb.vel.to_numpy().copy()
         step, prologue = step_fn(lb, me, coll, be, sc, bsc, kind)
@@ -478,6 +544,15 @@ def run_case(ref_root, name, spec, out_dir):
         out["psi"] = sc.psi_field.to_numpy()[:, :, 0]
         out["sc_force"] = lb.SCforce.to_numpy()[:, :, 0, :]
         out["T"] = lb.T.to_numpy()
+    if builder == "shanchen_mc":  # every component, [i, j, component, ...]
+        out["init_rho_mc"] = init_rho_all
+        out["f_mc"] = lb.f.to_numpy()
+        out["f2_mc"] = lb.f2.to_numpy()
+        out["rho_mc"] = lb.rho.to_numpy()
+        out["psi_mc"] = sc.psi_field.to_numpy()
+        out["sc_force_mc"] = lb.SCforce.to_numpy()
+        out["body_force_mc"] = lb.body_force.to_numpy()
+        out["pressure_mc"] = lb.pressure.to_numpy()
     out["meta"] = np.array(json.dumps(case.meta))
     np.savez_compressed(os.path.join(out_dir, name + ".npz"), **out)
     return time.time() - t0
