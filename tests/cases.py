@@ -27,9 +27,10 @@ def load_fixture(name):
 
 
 def fixture_names():
-    """Single-component fixtures (the multi-component ones, mc_*, have their
-    own oracle and test)."""
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("mc_"))
+    """Fixtures of the single-component step (the multi-component ones, mc_*,
+    and the immersed-boundary ones, ibm_*, have their own oracles and tests)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith(("mc_", "ibm_")))
 
 
 def _member_fn(nodes, nx, ny):

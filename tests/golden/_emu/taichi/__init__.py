@@ -221,8 +221,84 @@ def data_oriented(cls):
     return cls
 
 
+class StructField:
+    """A field of ti.dataclass structs: one Field per member."""
+
+    def __init__(self, members, shape, offset=None):
+        object.__setattr__(self, "_members",
+                           {name: Field(dt, shape, elem, offset) for name, (elem, dt) in members.items()})
+
+    def __getitem__(self, key):
+        return _StructRef(self, key)
+
+    def __getattr__(self, name):
+        try:
+            return object.__getattribute__(self, "_members")[name]
+        except KeyError:
+            raise AttributeError(name) from None
+
+    def __iter__(self):
+        return iter(next(iter(self._members.values())))
+
+
+class _StructRef:
+    """One struct of a StructField: members read as views (so .x/.y writes land
+    in the field) and assignments write through."""
+
+    __slots__ = ("_sf", "_key")
+
+    def __init__(self, sf, key):
+        object.__setattr__(self, "_sf", sf)
+        object.__setattr__(self, "_key", key)
+
+    def __getattr__(self, name):
+        f = self._sf._members[name]
+        idx = f._idx(self._key)
+        if f.elem:
+            return f.arr[idx].view(Vec)
+        r = f.arr[idx]
+        return int(r) if np.issubdtype(f.dtype, np.integer) else f.dtype(r)
+
+    def __setattr__(self, name, value):
+        f = self._sf._members[name]
+        f.arr[f._idx(self._key)] = value
+
+
 def dataclass(cls):
+    """Struct types: Cls.field(shape=...) gives a StructField whose members
+    follow the annotations (ti.math.vec2/vec3 vectors, int, float)."""
+    ann = dict(getattr(cls, "__annotations__", {}))
+
+    def field(shape=(), offset=None, **kwargs):
+        members = {}
+        for name, a in ann.items():
+            if a in ("vec2", "vec3"):
+                members[name] = ((int(a[-1]),), float)
+            elif a is int:
+                members[name] = ((), int)
+            else:
+                members[name] = ((), float)
+        return StructField(members, shape, offset)
+
+    cls.field = staticmethod(field)
     return cls
+
+
+def ndrange(*ranges):
+    import itertools
+    return itertools.product(*[range(*r) if isinstance(r, tuple) else range(r) for r in ranges])
+
+
+def cast(x, dtype):
+    return int(x) if dtype is int else _dtype(dtype)(x)
+
+
+def round(x):  # noqa: A001  (taichi's name)
+    return np.round(x)
+
+
+def abs(x):  # noqa: A001  (taichi's name)
+    return np.abs(x)
 
 
 def _ti_ipow(a, n):

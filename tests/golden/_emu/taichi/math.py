@@ -40,3 +40,11 @@ def cos(x):
 
 def sin(x):
     return np.sin(x)
+
+
+def floor(x):
+    return np.floor(x)
+
+
+def ceil(x):
+    return np.ceil(x)

@@ -358,6 +358,45 @@ def build_shanchen_mc(ti, tl, case, nx, ny, *, g_coh, rho_init, nu, rho0, T=1.0,
     return lb, me, coll, be, lb.sc_field, bsc
 
 
+def build_ibm_box(ti, tl, case, nx, ny, *, center, radius, mdf, nu, gravity):
+    """Fully periodic box driven by gravity past one immersed circle (SphereIB
+    with IB nodes every unit of arc, IBDEMCouplerEngine placing them, IBEngine
+    multi-direct forcing with `mdf` iterations), BGK, the IB step between the
+    velocity and the collision (ibm.py)."""
+    lb = tl.LBField(case.meta["name"], nx, ny, 1)
+    lb.set_gravity(ti.Vector(list(gravity)))
+    case.meta["gravity"] = list(gravity)
+    be = tl.BoundaryEngine()
+    cls = tl.BoundaryClassifier(ti.field(float, shape=(nx, ny)))
+
+    @ti.func
+    def fluid_fn(i, j):
+        return lb.mask[i, j] == 1
+    fluid = tl.FluidBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    fluid.precompute(classifier=cls)
+    be.add_boundary_condition("fluid", fluid)
+    case.bc("fluid", "fluid", group_nodes(fluid.group))
+    per = tl.PeriodicAllBoundary(spec=tl.BoundarySpec(geometry_fn=fluid_fn))
+    per.precompute(classifier=cls)
+    be.add_boundary_condition("stream", per)
+    case.bc("stream", "periodic", group_nodes(per.group))
+    lb.neighbor_classify()
+    me = tl.MacroscopicEngine(fluid.group)
+    coll = make_collision(ti, tl, case, lb, fluid.group, ("bgk", {}), nu, None, None, None)
+    sphere = tl.SphereIB(1, 64)
+    sphere.init_Balls(1, np.array([0]), np.array([list(center)]), np.array([[0.0, 0.0]]), np.array([[0.0, 0.0]]),
+                      np.array([0.0]), np.array([radius]), np.array([0.0]))
+    sphere.init_IB_nodes()
+    coupler = tl.IBDEMCouplerEngine(lb)
+    coupler.SphereInfoUpdata(sphere, np.array([list(center)]), np.array([[0.0, 0.0]]), np.array([0.0]))
+    ib = tl.IBEngine(mdf)
+    case.meta["ibm"] = {"center": list(center), "radius": radius, "mdf": mdf}
+    for (i, j) in group_nodes(fluid.group):
+        lb.rho[i, j, 0] = 1.0
+    lb.init_LBM(coll, fluid.group)
+    return lb, me, coll, be, (sphere, ib), None
+
+
 def step_fn(lb, me, coll, be, sc, bsc, kind):
     def standard():
         me.density(lb)
@@ -388,6 +427,25 @@ def step_fn(lb, me, coll, be, sc, bsc, kind):
         coll.apply(lb)
         be.apply_boundary_conditions(lb)
         me.time_updata(lb)
+
+    def ibm():
+        sphere, ib = sc
+        me.density(lb)
+        me.pressure(lb)
+        me.force_density(lb)
+        me.velocity(lb)
+        ib.MultiDirectForcingLoop(sphere, lb)
+        ib.ComputeParticleForce(sphere)
+        coll.apply(lb)
+        be.apply_boundary_conditions(lb)
+
+    if kind == "ibm":
+        def prologue():
+            me.density(lb)
+            me.pressure(lb)
+            me.force_density(lb)
+            me.velocity(lb)
+        return ibm, prologue
 
     def prologue():
         me.density(lb)
@@ -493,6 +551,8 @@ def case_table():
                                                     nu=(1.0 / 6.0, 0.1), rho0=(1.0, 1.0),
                                                     gravity=(0.0, -1e-5) if fp == "f32" else None),
                                  "shanchen", 30, fp, (mx, my))
+    t["ibm_circle_bgk_f32"] = ("ibm", dict(center=(16.0, 12.0), radius=4.0, mdf=2, nu=0.1,
+                                           gravity=(1e-5, 0.0)), "ibm", 30, "f32", (32, 24))
     return t
 
 
@@ -509,6 +569,8 @@ def run_case(ref_root, name, spec, out_dir):
             lb, me, coll, be, sc, bsc = build_channel(ti, tl, case, nx, ny, **kw)
         elif builder == "shanchen_mc":
             lb, me, coll, be, sc, bsc = build_shanchen_mc(ti, tl, case, nx, ny, **kw)
+        elif builder == "ibm":
+            lb, me, coll, be, sc, bsc = build_ibm_box(ti, tl, case, nx, ny, **kw)
         else:
             lb, me, coll, be, sc, bsc = build_shanchen(ti, tl, case, nx, ny, **kw)
         init_rho_all = lb.rho.to_numpy().copy()
@@ -540,6 +602,14 @@ def run_case(ref_root, name, spec, out_dir):
     else:
         out["diag"] = coll.diag.to_numpy()[:, :, 0, :]
         out["M_inverse"] = coll.M_inverse.to_numpy()
+    if builder == "ibm":  # the immersed circle's nodes and the resultant
+        sphere, _ = sc
+        for k in ("pos", "vel", "vel_desired", "force", "force_temp"):
+            out["ib_" + k] = getattr(sphere.IBNodes, k).to_numpy()[0, :sphere.Sphere[0].NumIB]
+        out["ib_count"] = np.array(sphere.IBInsiderCount[None])
+        out["sphere_force"] = sphere.Sphere.force.to_numpy()[0]
+        out["sphere_torque"] = np.array(sphere.Sphere.torque.to_numpy()[0])
+        sc = None
     if sc is not None:
         out["psi"] = sc.psi_field.to_numpy()[:, :, 0]
         out["sc_force"] = lb.SCforce.to_numpy()[:, :, 0, :]
