@@ -102,6 +102,17 @@ typedef struct LbmLattice {
   float gravity[2];   /* LBField.gravity_force                              */
 } LbmLattice;
 
+/* Immersed-boundary nodes (taichi_lbm/ibm.py:7-14, the IBMNodes fields),
+ * n nodes as [n][2] float arrays in device memory. */
+typedef struct LbmIBNodes {
+  int64_t n;
+  float* pos;
+  float* vel;
+  float* vel_desired;
+  float* force;
+  float* force_temp;
+} LbmIBNodes;
+
 /* Collision operator state (taichi_lbm/CollisionEngine.py:6-451). */
 typedef struct LbmCollision {
   int32_t model;        /* LBM_BGK / LBM_TRT / LBM_MRT                           */
@@ -161,6 +172,15 @@ int lbm_pressure(const LbmLattice* lat, const int32_t* group, int64_t n, int32_t
 int lbm_force_density(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
 /* MacroscopicEngine.velocity — taichi_lbm/lbm.py:223-237 */
 int lbm_velocity(const LbmLattice* lat, const int32_t* group, int64_t n, void* stream);
+
+/* IBEngine.InterpolateBodyVelocities — taichi_lbm/ibm.py:201-223: each node's
+ * velocity from the lattice velocity on its floor..ceil stencil, and its
+ * correction force 2 (vel_desired - vel) into force_temp, added to force. */
+int lbm_ibm_interpolate(const LbmLattice* lat, const LbmIBNodes* nodes, void* stream);
+/* IBEngine.SpreadBodyForces — taichi_lbm/ibm.py:225-246: each node's
+ * force_temp spread on its stencil into the lattice velocity (/ 2 total_rho)
+ * and body force (x rho / total_rho).  Adds are atomic. */
+int lbm_ibm_spread(const LbmLattice* lat, const LbmIBNodes* nodes, void* stream);
 
 /* {BGK,TRT,MRT}Collision.initTau — CollisionEngine.py:65-70, 149-155, 301-318 */
 int lbm_collision_init_tau(const LbmLattice* lat, const LbmCollision* c, const int32_t* group,

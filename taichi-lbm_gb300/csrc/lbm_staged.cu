@@ -489,7 +489,78 @@ __global__ void k_open_conv2(LbmLattice L, LbmBoundary b, const int32_t* g, int6
   L.psi[psi_at(L, i, j)] = eos_psi(b.eos, L.rho[q], L.temperature[q]);
 }
 
-int check_lat(const LbmLattice* L, bool need_f = true) {
+int check_lat(const LbmLattice* L, bool need_f = true);
+
+// ------------------------------------------------------------ immersed boundary
+// IBEngine (taichi_lbm/ibm.py:187-246): one thread per IB node.  The stencil
+// of a node at (px, py) is the grid nodes floor..ceil in each direction
+// (ibm.py:187-194) with weights (1 - |px - i|)(1 - |py - j|) (ibm.py:196-199).
+// Stencil nodes outside the lattice are skipped: the reference's insider
+// rule keeps nodes strictly inside, and reads there are undefined in it.
+__device__ inline float ib_weight(float px, float py, int ix, int iy) {
+  return (1.0f - fabsf(px - (float)ix)) * (1.0f - fabsf(py - (float)iy));
+}
+
+// InterpolateBodyVelocities (ibm.py:201-223)
+__global__ void k_ibm_interpolate(LbmLattice L, LbmIBNodes N) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= N.n) return;
+  const Idx I = idx_of(L);
+  const float px = N.pos[2 * m], py = N.pos[2 * m + 1];
+  const int xb = (int)floorf(px), yb = (int)floorf(py), xt = (int)ceilf(px), yt = (int)ceilf(py);
+  float vx = 0.0f, vy = 0.0f;
+  for (int ix = xb; ix <= xt; ++ix)
+    for (int iy = yb; iy <= yt; ++iy) {
+      if (ix < 0 || ix >= L.nx || iy < 0 || iy >= L.ny) continue;
+      const float w = ib_weight(px, py, ix, iy);
+      const size_t q = I.at(ix, iy);
+      vx += L.vel[q] * w;
+      vy += L.vel[I.plane + q] * w;
+    }
+  N.vel[2 * m] = vx;
+  N.vel[2 * m + 1] = vy;
+  const float fx = 2.0f * (N.vel_desired[2 * m] - vx), fy = 2.0f * (N.vel_desired[2 * m + 1] - vy);
+  N.force_temp[2 * m] = fx;
+  N.force_temp[2 * m + 1] = fy;
+  N.force[2 * m] += fx;
+  N.force[2 * m + 1] += fy;
+}
+
+// SpreadBodyForces (ibm.py:225-246): several IB nodes add into one grid node,
+// so the adds are atomic (the reference's parallel loop adds in an arbitrary
+// order as well)
+__global__ void k_ibm_spread(LbmLattice L, LbmIBNodes N) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= N.n) return;
+  const Idx I = idx_of(L);
+  const float px = N.pos[2 * m], py = N.pos[2 * m + 1];
+  const int xb = (int)floorf(px), yb = (int)floorf(py), xt = (int)ceilf(px), yt = (int)ceilf(py);
+  for (int ix = xb; ix <= xt; ++ix)
+    for (int iy = yb; iy <= yt; ++iy) {
+      if (ix < 0 || ix >= L.nx || iy < 0 || iy >= L.ny) continue;
+      const float w = ib_weight(px, py, ix, iy);
+      const size_t q = I.at(ix, iy);
+      const float tx = 0.0f + N.force_temp[2 * m] * w, ty = 0.0f + N.force_temp[2 * m + 1] * w;
+      const float r2 = L.total_rho[q] * 2.0f;
+      atomicAdd(&L.vel[q], tx / r2);
+      atomicAdd(&L.vel[I.plane + q], ty / r2);
+      atomicAdd(&L.body_force[q], (tx * L.rho[q]) / L.total_rho[q]);
+      atomicAdd(&L.body_force[I.plane + q], (ty * L.rho[q]) / L.total_rho[q]);
+    }
+}
+
+int check_ib(const LbmLattice* L, const LbmIBNodes* N) {
+  int rc = check_lat(L, false);
+  if (rc) return rc;
+  if (!L->vel || !L->rho || !L->total_rho || !L->body_force)
+    return lbm_err::set(LBM_ERR_ARG, "immersed boundary needs vel, rho, total_rho and body_force");
+  if (!N || N->n < 0) return lbm_err::set(LBM_ERR_ARG, "IB nodes missing or negative count");
+  if (N->n > 0 && (!N->pos || !N->vel || !N->vel_desired || !N->force || !N->force_temp))
+    return lbm_err::set(LBM_ERR_ARG, "IB node arrays missing");
+  return LBM_OK;
+}
+
+int check_lat(const LbmLattice* L, bool need_f) {
   if (!L) return lbm_err::set(LBM_ERR_ARG, "lattice is NULL");
   if (L->nx <= 0 || L->ny <= 0 || L->pitch < L->nx)
     return lbm_err::set(LBM_ERR_ARG, "bad lattice shape %d x %d pitch %d", L->nx, L->ny, L->pitch);
@@ -547,6 +618,18 @@ int lbm_pressure(const LbmLattice* L, const int32_t* g, int64_t n, int32_t with_
   fill(L->pressure, (size_t)L->ny * L->pitch, 0.0f, S_);
   if (n) k_pressure<<<blocks_for(n), TPB, 0, S_>>>(*L, g, n, with_sc, g_coh);
   return lbm_err::launch("pressure");
+}
+
+int lbm_ibm_interpolate(const LbmLattice* L, const LbmIBNodes* N, void* stream) {
+  CHECK(check_ib(L, N));
+  if (N->n) k_ibm_interpolate<<<blocks_for(N->n), TPB, 0, S_>>>(*L, *N);
+  return lbm_err::launch("ibm_interpolate");
+}
+
+int lbm_ibm_spread(const LbmLattice* L, const LbmIBNodes* N, void* stream) {
+  CHECK(check_ib(L, N));
+  if (N->n) k_ibm_spread<<<blocks_for(N->n), TPB, 0, S_>>>(*L, *N);
+  return lbm_err::launch("ibm_spread");
 }
 
 int lbm_force_density(const LbmLattice* L, const int32_t* g, int64_t n, void* stream) {

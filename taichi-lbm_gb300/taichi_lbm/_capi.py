@@ -33,6 +33,10 @@ class LbmLattice(ctypes.Structure):
                            "mask", "links")] + [("gravity", ctypes.c_float * 2)]
 
 
+class LbmIBNodes(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64)] + [(n, _vp) for n in ("pos", "vel", "vel_desired", "force", "force_temp")]
+
+
 class LbmCollision(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int32), ("fluid_model", ctypes.c_int32),
                 ("nu", ctypes.c_float), ("nu_bulk", ctypes.c_float), ("magic", ctypes.c_float),
@@ -98,6 +102,8 @@ _SIGS = {
                       ctypes.c_float, _vp], ctypes.c_int),
     "lbm_force_density": ([ctypes.POINTER(LbmLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
     "lbm_velocity": ([ctypes.POINTER(LbmLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_ibm_interpolate": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmIBNodes), _vp], ctypes.c_int),
+    "lbm_ibm_spread": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmIBNodes), _vp], ctypes.c_int),
     "lbm_collision_init_tau": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmCollision), _vp,
                                 ctypes.c_int64, _vp], ctypes.c_int),
     "lbm_collision_shear_rate": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmCollision), _vp,

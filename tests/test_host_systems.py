@@ -97,3 +97,30 @@ def test_replica_timing_takes_the_slowest_rank():
     out = mp.Manager().dict()
     mp.spawn(_replica_rank, args=(2, port, out), nprocs=2, join=True)
     assert out[0] == out[1] == 5.0
+
+
+def test_ib_node_placement_matches_reference(built):
+    """SphereIB / IBDEMCouplerEngine place the IB nodes and list the insiders
+    exactly as the reference's ibm.py did for the immersed-circle fixture
+    (host work; device tensors on the CPU here)."""
+    import types
+    from taichi_lbm.ibm import IBDEMCouplerEngine, IBEngine, SphereIB
+    d = np.load(f"{ROOT}/tests/golden/ibm_circle_bgk_f32.npz")
+    meta = json.loads(str(d["meta"]))
+    ib = meta["ibm"]
+    s = SphereIB(1, 64, device="cpu")
+    c = np.array([ib["center"]])
+    s.init_Balls(1, np.array([0]), c, np.zeros((1, 2)), np.zeros((1, 2)), np.zeros(1), np.array([ib["radius"]]),
+                 np.zeros(1))
+    s.init_IB_nodes()
+    eng = IBDEMCouplerEngine(types.SimpleNamespace(NX=meta["NX"], NY=meta["NY"]))
+    eng.SphereInfoUpdata(s, c, np.zeros((1, 2)), np.zeros(1))
+    n = int(s.Sphere.NumIB[0])
+    assert s.IBInsiderCount[None] == int(d["ib_count"]) == n
+    assert np.array_equal(s.IBNodes.pos.to_numpy()[0, :n], d["ib_pos"])
+    # ComputeParticleForce: the resultant is the last insider node's force
+    f = np.zeros((1, 64, 2), np.float32)
+    f[0, :n] = np.arange(2 * n, dtype=np.float32).reshape(n, 2)
+    s.IBNodes.force.from_numpy(f)
+    IBEngine(1).ComputeParticleForce(s)
+    assert np.array_equal(s.Sphere.force.to_numpy()[0], f[0, n - 1])
