@@ -5,7 +5,7 @@ same as running it alone through FusedSolver.step(n, forces=True)."""
 import numpy as np
 import pytest
 
-from tests.cases import fields_of, rel_err
+from tests.cases import rel_err
 
 pytestmark = pytest.mark.gpu
 
