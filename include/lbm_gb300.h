@@ -195,14 +195,14 @@ int lbm_collision_relaxation_time(const LbmLattice* lat, const LbmCollision* c,
 int lbm_collision_apply(const LbmLattice* lat, const LbmCollision* c, const int32_t* group,
                         int64_t n, void* stream);
 
-/* ShanChenForceC1.update_psi — taichi_lbm/ExternalForce.py:137-142 */
+/* ShanChenForceC1.update_psi — taichi_lbm/ExternalForce.py:42-47 */
 int lbm_sc_update_psi(const LbmLattice* lat, const LbmEos* eos, const int32_t* group, int64_t n,
                       void* stream);
-/* ShanChenForceC1.cau_SCforce — taichi_lbm/ExternalForce.py:145-158 */
+/* ShanChenForceC1.cau_SCforce — taichi_lbm/ExternalForce.py:50-63 */
 int lbm_sc_force(const LbmLattice* lat, float g_coh, const int32_t* group, int64_t n, void* stream);
-/* PeriodicPsi_LR (axis 0) / PeriodicPsi_BT (axis 1) — SCBoundaryCondition.py:365-383 */
+/* PeriodicPsi_LR (axis 0) / PeriodicPsi_BT (axis 1) — SCBoundaryCondition.py:126-144 */
 int lbm_psi_periodic(const LbmLattice* lat, int32_t axis, void* stream);
-/* FixedPsi.apply — SCBoundaryCondition.py:352-362 */
+/* FixedPsi.apply — SCBoundaryCondition.py:119-123 */
 int lbm_psi_fixed(const LbmLattice* lat, const int32_t* group, int64_t n, float value, void* stream);
 
 /* <BoundaryCondition>.apply for every kind in LBM_BC_* —
@@ -267,7 +267,7 @@ typedef struct LbmPlanDesc {
                            0..LBM_PREFETCH_TUNINGS-1 selects
                            (8,2) (8,3) (4,4) (16,2) for the plain segments'
                            shared-memory ring                               */
-  /* Single-component Shan-Chen (ExternalForce.py:122-158) on a fully periodic
+  /* Single-component Shan-Chen (ExternalForce.py:27-63) on a fully periodic
    * lattice: each step computes psi(rho, T) from the post-stream populations,
    * F = -g_coh psi(x) sum_k w_k c_k psi(x + c_k) + gravity, then collides.
    * Needs the direct pipeline, nodes_per_thread 4, no
@@ -378,10 +378,14 @@ int lbm_plan_reduce_moments(LbmPlan* plan, double* partials, double* out, void* 
  * Scratch is a 48 KiB file-scope __device__ array that every GPU which loads
  * the library holds until process exit.  The first call on each device looks
  * its device address up (cudaGetSymbolAddress) with that device current, so
- * make that first call before any stream capture.  Lattices with more than
- * LBM_NOALLOC_MAX_NODES sites (ny * pitch) are rejected with LBM_ERR_ARG.
- * Every call shares the array: calls that overlap on the GPU race.  No
- * cudaMalloc, cudaFree or allocating library routine is called. */
+ * make that first call before any stream capture.  The address is kept for
+ * the process's life and belongs to the device's primary context (the one
+ * the CUDA runtime and PyTorch use): calls from another driver context, or
+ * after cudaDeviceReset, are not supported.  Lattices with more than
+ * LBM_NOALLOC_MAX_NODES sites (ny * pitch) are rejected with LBM_ERR_ARG
+ * before the plan's buffers are looked at, so an unbound plan is rejected
+ * the same way.  Every call shares the array: calls that overlap on the GPU
+ * race.  No cudaMalloc, cudaFree or allocating library routine is called. */
 #define LBM_NOALLOC_CHUNK 16384LL
 #define LBM_NOALLOC_MAX_NODES (2048LL * LBM_NOALLOC_CHUNK)
 int lbm_plan_reduce_moments_noalloc(LbmPlan* plan, double* out, void* stream);

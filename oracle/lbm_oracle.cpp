@@ -521,7 +521,7 @@ void mrt_apply(Lattice<T>& L, const int32_t* g, int64_t n) {
 }
 
 // ---------------------------------------------------------------- Shan-Chen
-// ExternalForce.py:137-142
+// ExternalForce.py:42-47
 template <class T>
 void sc_update_psi(Lattice<T>& L, const int32_t* g, int64_t n, EosParams e) {
 #pragma omp parallel for
@@ -531,7 +531,7 @@ void sc_update_psi(Lattice<T>& L, const int32_t* g, int64_t n, EosParams e) {
   }
 }
 
-// SCBoundaryCondition.py:366-383 — periodic psi halo, LR then BT
+// SCBoundaryCondition.py:126-144 — periodic psi halo, LR then BT
 template <class T>
 void psi_periodic_lr(Lattice<T>& L) {
   for (int y = -1; y <= L.NY; ++y) {
@@ -547,13 +547,13 @@ void psi_periodic_bt(Lattice<T>& L) {
   }
 }
 
-// SCBoundaryCondition.py:358-362 — FixedPsi
+// SCBoundaryCondition.py:113-123 — FixedPsi
 template <class T>
 void psi_fixed(Lattice<T>& L, const int32_t* g, int64_t n, double value) {
   for (int64_t m = 0; m < n; ++m) L.psi[L.pid(g[2 * m], g[2 * m + 1])] = T(value);
 }
 
-// SC force at one node (ExternalForce.py:150-158 and BoundaryCondition.py:301-312)
+// SC force at one node (ExternalForce.py:50-63 and BoundaryCondition.py:301-312)
 template <class T>
 void sc_force_node(Lattice<T>& L, int i, int j, T g_coh) {
   T Fx = T(0), Fy = T(0);
@@ -571,7 +571,7 @@ void sc_force_node(Lattice<T>& L, int i, int j, T g_coh) {
   L.scforce[2 * q + 1] = T(0) + Fy;
 }
 
-// ExternalForce.py:145-158
+// ExternalForce.py:50-63
 template <class T>
 void sc_force(Lattice<T>& L, const int32_t* g, int64_t n, double g_coh) {
   std::fill(L.scforce.begin(), L.scforce.end(), T(0));

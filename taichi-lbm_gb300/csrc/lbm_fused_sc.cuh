@@ -2,9 +2,9 @@
 //
 // The reference's Shan-Chen step (cases/Bubble or two-phase separation.py:
 // 197-212) computes, from the post-stream populations of every node,
-// rho -> psi(rho, T) (EOS.py:28-47, ExternalForce.py:137-142), wraps psi
-// periodically (SCBoundaryCondition.py:365-383), then the force
-// F(x) = -g psi(x) sum_k w_k c_k psi(x + c_k) (ExternalForce.py:145-158),
+// rho -> psi(rho, T) (EOS.py:28-47, ExternalForce.py:42-47), wraps psi
+// periodically (SCBoundaryCondition.py:126-144), then the force
+// F(x) = -g psi(x) sum_k w_k c_k psi(x + c_k) (ExternalForce.py:50-63),
 // F_body = F + rho/rho_tot g (lbm.py:215-220), the velocity and the
 // collision.  A node's force needs psi of its eight neighbours in the same
 // step.  Here one warp owns a strip of 32*V columns and SC_CHUNK rows and

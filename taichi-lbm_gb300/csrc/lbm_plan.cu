@@ -388,7 +388,10 @@ __device__ __align__(256) double g_noalloc_partials[3 * LBM_NOALLOC_BLOCKS];
 
 // Host code cannot use g_noalloc_partials as a pointer: its host-side name is
 // a stand-in, not the device address.  The address is looked up once per
-// device, with that device current, on the first call made on it.
+// device, with that device current, on the first call made on it, and kept
+// for the life of the process.  It belongs to the device's primary context
+// (the one the CUDA runtime and PyTorch use): after cudaDeviceReset, or from
+// another driver context, the kept address no longer names the array.
 constexpr int MAX_DEVICES = 64;
 double* g_noalloc_ptr[MAX_DEVICES] = {nullptr};
 std::mutex g_noalloc_mutex;
@@ -461,14 +464,16 @@ int launch_noalloc(const FusedParams& p, double* partials, int nblocks, double* 
 extern "C" {
 
 int lbm_plan_reduce_moments_noalloc(LbmPlan* pl, double* out, void* stream) {
-  if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "reduce_noalloc: plan not bound");
-  if (!out) return lbm_err::set(LBM_ERR_ARG, "reduce_noalloc: NULL output");
+  if (!pl) return lbm_err::set(LBM_ERR_ARG, "reduce_noalloc: NULL plan");
+  // the size is the descriptor's: checked before anything bound is looked at
   const int64_t sites = (int64_t)pl->d.ny * pl->d.pitch;
   if (sites > LBM_NOALLOC_MAX_NODES)
     return lbm_err::set(LBM_ERR_ARG,
                         "reduce_noalloc: lattice of %lld sites (ny * pitch) exceeds the allocation-free "
                         "limit of %lld; use lbm_plan_reduce_moments with caller scratch",
                         (long long)sites, (long long)LBM_NOALLOC_MAX_NODES);
+  if (!pl->bound) return lbm_err::set(LBM_ERR_STATE, "reduce_noalloc: plan not bound");
+  if (!out) return lbm_err::set(LBM_ERR_ARG, "reduce_noalloc: NULL output");
   double* partials = nullptr;
   int rc = noalloc_scratch(&partials);
   if (rc) return rc;

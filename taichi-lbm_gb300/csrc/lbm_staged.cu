@@ -256,7 +256,7 @@ __global__ void k_collide(LbmLattice L, LbmCollision c, const int32_t* g, int64_
 }
 
 // --------------------------------------------------------------- Shan-Chen
-// ExternalForce.py:137-142
+// ExternalForce.py:42-47
 __global__ void k_update_psi(LbmLattice L, LbmEos e, const int32_t* g, int64_t n) {
   int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= n) return;
@@ -266,7 +266,7 @@ __global__ void k_update_psi(LbmLattice L, LbmEos e, const int32_t* g, int64_t n
   L.psi[psi_at(L, i, j)] = eos_psi(e, L.rho[q], L.temperature[q]);
 }
 
-// SC force at one node, ExternalForce.py:150-158 / BoundaryCondition.py:301-312
+// SC force at one node, ExternalForce.py:50-63 / BoundaryCondition.py:301-312
 __device__ inline void sc_force_node(const LbmLattice& L, const Idx& I, int i, int j, float g_coh) {
   float Fx = 0.0f, Fy = 0.0f;
 #pragma unroll
@@ -288,7 +288,7 @@ __global__ void k_sc_force(LbmLattice L, float g_coh, const int32_t* g, int64_t 
   sc_force_node(L, I, g[2 * m], g[2 * m + 1], g_coh);
 }
 
-// SCBoundaryCondition.py:365-383
+// SCBoundaryCondition.py:126-144
 __global__ void k_psi_periodic(LbmLattice L, int axis) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (axis == 0) {  // PeriodicPsi_LR: y in [-1, NY]
@@ -304,7 +304,7 @@ __global__ void k_psi_periodic(LbmLattice L, int axis) {
   }
 }
 
-// SCBoundaryCondition.py:358-362
+// SCBoundaryCondition.py:119-123
 __global__ void k_psi_fixed(LbmLattice L, const int32_t* g, int64_t n, float v) {
   int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= n) return;

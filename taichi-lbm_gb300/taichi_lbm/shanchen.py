@@ -114,7 +114,7 @@ class CS_psi(Pseudopotential):
 
 
 class ShanChenModel:
-    """ExternalForce.py:5-27: psi on a one-node halo around the lattice."""
+    """ExternalForce.py:5-23: psi on a one-node halo around the lattice."""
 
     def __init__(self, lb_field, group):
         self.group = group
@@ -123,7 +123,7 @@ class ShanChenModel:
 
 
 class ShanChenForceC1(ShanChenModel):
-    """ExternalForce.py:122-158: single-component Shan-Chen force."""
+    """ExternalForce.py:27-63: single-component Shan-Chen force."""
 
     def __init__(self, params):
         p = {"lb_field": None, "g_coh": None, "group": None, "psi": None}
@@ -147,7 +147,7 @@ class ShanChenForceC1(ShanChenModel):
 
 
 class ShanChenForceC2(ShanChenModel):
-    """ExternalForce.py:161-212 (two components) — not part of this build."""
+    """ExternalForce.py:66-117 (two components) — not part of this build."""
 
     def __init__(self, params):
         raise NotImplementedError("two-component Shan-Chen (ShanChenForceC2) is not built; "
@@ -156,7 +156,7 @@ class ShanChenForceC2(ShanChenModel):
 
 # ------------------------------------------------------------ psi boundaries
 class PeriodicPsi_LR:
-    """SCBoundaryCondition.py:365-373"""
+    """SCBoundaryCondition.py:126-134"""
 
     def apply(self, lb_field):
         L = lb_field._lattice()
@@ -164,7 +164,7 @@ class PeriodicPsi_LR:
 
 
 class PeriodicPsi_BT:
-    """SCBoundaryCondition.py:375-383"""
+    """SCBoundaryCondition.py:136-144"""
 
     def apply(self, lb_field):
         L = lb_field._lattice()
@@ -172,7 +172,7 @@ class PeriodicPsi_BT:
 
 
 class FixedPsi(BoundaryCondition):
-    """SCBoundaryCondition.py:352-362"""
+    """SCBoundaryCondition.py:113-123"""
 
     def __init__(self, spec, psi_value):
         super().__init__(spec)
@@ -185,7 +185,7 @@ class FixedPsi(BoundaryCondition):
 
 
 class OpenBoundaryPsi(PlaneBoundary):
-    """SCBoundaryCondition.py:9-16.  The open psi boundaries
+    """SCBoundaryCondition.py:9-15.  The open psi boundaries
     (OpenNeumannPsi, OpenConvective1orderPsi, OpenConvective2orderPsi,
     OpenExtrapolationPsi) have no CUDA kernel in this build."""
 
@@ -210,7 +210,7 @@ class OpenExtrapolationPsi(OpenBoundaryPsi):
 
 
 class BoundaryEngineSC:
-    """SCBoundaryCondition.py:388-399"""
+    """SCBoundaryCondition.py:149-160"""
 
     def __init__(self):
         self.boundary_conditions = {}

@@ -19,7 +19,8 @@ After ``steps`` calls of the case's step function the driver runs the moment
 prologue of the next step (density, pressure, [psi, SC force], force_density,
 velocity) and records every field: that is the comparison point.
 
-Usage:  python tests/golden/make_golden.py [--ref PATH] [case ...]
+Usage:  python tests/golden/make_golden.py --ref PATH [case ...]
+        (or TAICHI_LBM_REF=PATH in the environment instead of --ref)
 """
 import argparse
 import contextlib
@@ -630,10 +631,13 @@ def run_case(ref_root, name, spec, out_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("TAICHI_LBM_REF"),
+                    help="checkout of the reference (default: $TAICHI_LBM_REF)")
     ap.add_argument("--out", default=HERE)
     ap.add_argument("cases", nargs="*")
     a = ap.parse_args()
+    if not a.ref:
+        raise SystemExit("give the reference checkout with --ref PATH or TAICHI_LBM_REF")
     table = case_table()
     names = a.cases or list(table)
     for n in names:

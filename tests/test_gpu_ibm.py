@@ -6,20 +6,15 @@ iterations between the velocity and the BGK collision, 30 steps), the case
 oracle/ibm.py reproduces bit for bit.  The spread adds atomically, so sums
 into a grid node shared by several IB nodes may round in another order:
 bound 1e-5 of each field's maximum.
-
-These kernels have not yet run on a GPU: the tests run when LBM_RUN_IBM_GPU=1.
 """
 import json
-import os
 
 import numpy as np
 import pytest
 
 from tests.cases import ROOT, rel_err
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("LBM_RUN_IBM_GPU") != "1",
-                                 reason="immersed-boundary kernels await their first GPU run")]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
