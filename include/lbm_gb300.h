@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define LBM_GB300_ABI_VERSION 2
+#define LBM_GB300_ABI_VERSION 3
 
 enum {
   LBM_OK = 0,
@@ -280,13 +280,38 @@ typedef struct LbmPlanDesc {
    * stored value is the small deviation from rest at density rho_ref; choose
    * the lattice's mean density (0 is read as 1).  Ignored for fp32.        */
   float rho_ref;
+  /* LBM_STORE_I16S: the step is 2^-fixed_exp, so stored deviations cover
+   * |f_k - w_k rho_ref| < 2^(15 - fixed_exp); 0 selects 19 (range 1/16).
+   * LBM_FIXED_EXP_MIN..LBM_FIXED_EXP_MAX.  Ignored by other storages.      */
+  int32_t fixed_exp;
+  /* LBM_PIPE_ASYNC: clock-cycle budget of each wait on a staged copy
+   * (0 selects about 2 s).  A wait that runs out sets LBM_STATUS_TIMEOUT;
+   * the copies still in flight are then waited for with the default budget
+   * before the kernel returns.                                             */
+  int64_t wait_cycles;
 } LbmPlanDesc;
+
+#define LBM_FIXED_EXP_DEFAULT 19
+#define LBM_FIXED_EXP_MIN 12
+#define LBM_FIXED_EXP_MAX 22
 
 enum { LBM_PIPE_DIRECT = 0, LBM_PIPE_ASYNC = 1, LBM_PIPE_PREFETCH = 2 };
 #define LBM_ASYNC_TUNINGS 4
 #define LBM_PREFETCH_TUNINGS 4
-/* *status (LbmPlanBuffers.status) after an async step: 0, or 1 when a wait on
- * a copy exceeded its time budget (the step's output is then invalid). */
+/* *status (LbmPlanBuffers.status) is a sticky set of bits that steps OR in
+ * and the caller clears:
+ *  LBM_STATUS_TIMEOUT    a wait on a staged copy (LBM_PIPE_ASYNC) exceeded
+ *                        its budget; the step's output is invalid
+ *  LBM_STATUS_SATURATED  LBM_STORE_I16S: a colliding node's post-collision
+ *                        value fell outside the fixed-point range (or was
+ *                        not finite) and was clamped
+ *  LBM_STATUS_NONFINITE  a colliding node's post-collision value was NaN or
+ *                        infinite (floating-point storages), or a drag/lift
+ *                        monitor summed to a non-finite force
+ * Only nodes inside the lattice whose code has LBM_CODE_ACTIVE are checked. */
+#define LBM_STATUS_TIMEOUT 1
+#define LBM_STATUS_SATURATED 2
+#define LBM_STATUS_NONFINITE 4
 
 typedef struct LbmPlanBuffers {
   void* fa;             /* [9][ny][pitch] populations, element type per storage */
@@ -299,7 +324,8 @@ typedef struct LbmPlanBuffers {
   const float* bc_vel;  /* [2][ny][pitch] per-node boundary velocity or NULL */
   float* tau;           /* [ny][pitch] power-law state (BGK tau, TRT tau_sym,
                            MRT diag[7]) or NULL                              */
-  int32_t* status;      /* one device int32 (LBM_PIPE_ASYNC), else NULL     */
+  int32_t* status;      /* one device int32 of LBM_STATUS_* bits; required
+                           by LBM_PIPE_ASYNC, optional (NULL) otherwise     */
   /* LBM_PIPE_DIRECT or LBM_PIPE_PREFETCH, optional: the indices (y * nseg + seg, ascending)
    * of every segment whose seg_flags entry is nonzero.  With it a step is two
    * launches, a lean kernel over the plain segments and a general one over

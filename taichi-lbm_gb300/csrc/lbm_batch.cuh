@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_batch_monitor(const BatchLattice* _
   for (int64_t i = threadIdx.x; i < m.nlinks; i += blockDim.x) {
     const int64_t q = m.links[2 * i];
     const int k = m.links[2 * i + 1];
-    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
+    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k], p.fq);
     fx += 2.0 * cx_dyn(k) * v;
     fy += 2.0 * cy_dyn(k) * v;
   }
@@ -175,6 +175,10 @@ __global__ void __launch_bounds__(MEX_TPB) k_batch_monitor(const BatchLattice* _
       m.series[2 * (size_t)c + 1] = sy;
     }
     *m.count = c + 1;
+    // a diverged member: its force is not finite (any NaN or infinity in
+    // the summed links reaches the total)
+    if (!(fabs(sx) <= 1.7976931348623157e308 && fabs(sy) <= 1.7976931348623157e308))
+      report_status(p.status, LBM_STATUS_NONFINITE);
   }
 }
 

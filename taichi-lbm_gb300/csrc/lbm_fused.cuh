@@ -66,6 +66,14 @@ struct FusedParams {
   float wsh[9];
   float rho_shift;  // sum_k wsh[k]
   float mwsh[9];    // MRT moments of the shift, M wsh
+  // fixed-point storage (LBM_STORE_I16S): step fq = 2^-e, its inverse fiq,
+  // and foff = (2^23 + 2^15) fq (the pair decode's offset)
+  float fq, fiq, foff;
+  // sticky device status word (LBM_STATUS_* bits), or null: stores that
+  // leave the fixed-point range or hold a non-finite value set a bit
+  int32_t* status;
+  // LBM_PIPE_ASYNC: clock-cycle budget of each wait on a staged copy
+  long long wait_cycles;
 };
 
 // The fields the lean (plain-segment) kernels read: a compact copy of
@@ -90,6 +98,8 @@ struct LeanParams {
   int sc_rows;  // rows of a strip item
   int model;    // collision model (batched kernels branch on it per lattice)
   const uint32_t* lane_mask;  // lanes not to store (FusedParams::lane_mask), or null
+  float fq, fiq, foff;        // fixed-point step (FusedParams::fq)
+  int32_t* status;            // FusedParams::status
 };
 
 // Division by an invariant divisor d (1 <= d < 2^31) as a multiply-high and
@@ -139,6 +149,10 @@ inline LeanParams lean_of(const FusedParams& f) {
   l.sc_rows = 16;
   l.model = f.model;
   l.lane_mask = f.lane_mask;
+  l.fq = f.fq;
+  l.fiq = f.fiq;
+  l.foff = f.foff;
+  l.status = f.status;
   return l;
 }
 
@@ -154,44 +168,49 @@ __device__ __forceinline__ void copy_words(T* dst, const T* src, int tid, int n)
 // ------------------------------------------------------------ storage
 template <int ST>
 struct Storage;
+// Every storage decodes with (stored value, shift w, fixed-point step q) and
+// encodes with (value, shift w, inverse step iq); only the fixed-point
+// storage reads q and iq.
 template <>
 struct Storage<LBM_STORE_F32> {
   using T = float;
-  static __device__ __forceinline__ float dec(T v, float) { return v; }
-  static __device__ __forceinline__ double dec64(T v, float) { return (double)v; }
-  static __device__ __forceinline__ T enc(float v, float) { return v; }
+  static __device__ __forceinline__ float dec(T v, float, float) { return v; }
+  static __device__ __forceinline__ double dec64(T v, float, float) { return (double)v; }
+  static __device__ __forceinline__ T enc(float v, float, float) { return v; }
 };
 template <>
 struct Storage<LBM_STORE_F16S> {
   using T = __half;
-  static __device__ __forceinline__ float dec(T v, float w) { return __half2float(v) + w; }
-  static __device__ __forceinline__ double dec64(T v, float w) { return (double)__half2float(v) + (double)w; }
-  static __device__ __forceinline__ T enc(float v, float w) { return __float2half_rn(v - w); }
+  static __device__ __forceinline__ float dec(T v, float w, float) { return __half2float(v) + w; }
+  static __device__ __forceinline__ double dec64(T v, float w, float) { return (double)__half2float(v) + (double)w; }
+  static __device__ __forceinline__ T enc(float v, float w, float) { return __float2half_rn(v - w); }
 };
 template <>
 struct Storage<LBM_STORE_BF16S> {
   using T = __nv_bfloat16;
-  static __device__ __forceinline__ float dec(T v, float w) { return __bfloat162float(v) + w; }
-  static __device__ __forceinline__ double dec64(T v, float w) { return (double)__bfloat162float(v) + (double)w; }
-  static __device__ __forceinline__ T enc(float v, float w) { return __float2bfloat16_rn(v - w); }
+  static __device__ __forceinline__ float dec(T v, float w, float) { return __bfloat162float(v) + w; }
+  static __device__ __forceinline__ double dec64(T v, float w, float) {
+    return (double)__bfloat162float(v) + (double)w;
+  }
+  static __device__ __forceinline__ T enc(float v, float w, float) { return __float2bfloat16_rn(v - w); }
 };
 
 // 16-bit fixed point, shifted (LBM_STORE_I16S): the state holds the integer
-// n = round((f_k - w_k rho_ref) / Q), Q = 2^-19, as int16, so |f_k - w_k
-// rho_ref| < 2^15 Q = 1/16.  Every stored value is a multiple of Q below
+// n = round((f_k - w_k rho_ref) / Q) as int16, with the plan's step
+// Q = 2^-e (LbmPlanDesc.fixed_exp, default e = 19), so |f_k - w_k rho_ref| <
+// 2^15 Q (1/16 at the default).  Every stored value is a multiple of Q below
 // 2^15 Q, so a sum of a node's nine values is exact in FP32 (9 * 2^15 <
 // 2^24): a collision can store its populations with their sum, the node's
 // mass, unchanged to the bit (i16_conserve_bits), which floating-point storage
 // cannot.  Rounding is to nearest even through the 1.5 * 2^23 magic
 // constant (x + 1.5 * 2^23 rounds x to an integer for |x| < 2^22); values
-// outside the range saturate.
-constexpr float I16_Q = 1.9073486328125e-06f;  // 2^-19
-constexpr float I16_IQ = 524288.0f;            // 2^19
-constexpr float I16_MAGIC = 12582912.0f;       // 1.5 * 2^23
+// outside the range saturate, and the store reports them.
+constexpr float I16_MAGIC = 12582912.0f;  // 1.5 * 2^23
+constexpr float I16_LO = I16_MAGIC - 32768.0f, I16_HI = I16_MAGIC + 32767.0f;
 
 // the nearest step count of a shifted value, saturated, as an integer float
-__device__ __forceinline__ float i16_steps(float h) {
-  const float n = fmaf(h, I16_IQ, I16_MAGIC) - I16_MAGIC;
+__device__ __forceinline__ float i16_steps(float h, float iq) {
+  const float n = fmaf(h, iq, I16_MAGIC) - I16_MAGIC;
   return fminf(fmaxf(n, -32768.0f), 32767.0f);
 }
 // an integer float in [-32768, 32767] -> its int16 bits (in the low half)
@@ -200,53 +219,77 @@ __device__ __forceinline__ unsigned i16_bits(float n) { return __float_as_uint(n
 template <>
 struct Storage<LBM_STORE_I16S> {
   using T = short;
-  static __device__ __forceinline__ float dec(T v, float w) { return fmaf((float)v, I16_Q, w); }
-  static __device__ __forceinline__ double dec64(T v, float w) { return (double)v * (double)I16_Q + (double)w; }
-  static __device__ __forceinline__ T enc(float v, float w) { return (short)i16_bits(i16_steps(v - w)); }
+  static __device__ __forceinline__ float dec(T v, float w, float q) { return fmaf((float)v, q, w); }
+  static __device__ __forceinline__ double dec64(T v, float w, float q) {
+    return (double)v * (double)q + (double)w;
+  }
+  static __device__ __forceinline__ T enc(float v, float w, float iq) { return (short)i16_bits(i16_steps(v - w, iq)); }
 };
 
 // Mass-conserving quantisation of one node's post-collision populations
 // for the fixed-point storage: populations 1..8 round to their nearest
 // step, and population 0 takes the rest of the node's pre-collision mass
 // d (a sum of stored values, exact), so the stored sum equals d exactly.
-// h: shifted post-collision values.  b[k]: the int16 bits of the stored
-// step counts in the low half of each word.  The rounding yields
+// Colliding nodes without a boundary program conserve so; so a closed
+// lattice keeps its mass to the bit.  A node whose populations a boundary
+// program rewrote passes the sum of its rounded post-collision values as d
+// instead (plain rounding to nearest): its boundary sets the mass that
+// crosses it, and conserving the rounded boundary values there biases the
+// mass an open channel carries, step after step, when its outlet does not
+// pin the density (PressureNEEM writes rho_value to total_rho only).
+// h: shifted post-collision values; iq = 1 / Q.  b[k]: the int16 bits of the
+// stored step counts in the low half of each word.  The rounding yields
 // t = n + 1.5 * 2^23 as a float, whose bit pattern is that of 1.5 * 2^23
 // plus n, so the step counts add up as integers without a conversion.
-__device__ __forceinline__ void i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9]) {
+// Returns true when a value left the range (saturated) or was not finite
+// (a NaN fails both range tests).
+__device__ __forceinline__ bool i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9], float iq) {
   const unsigned mb = __float_as_uint(I16_MAGIC);
   unsigned s = 0u;  // sum of the steps of populations 1..8 (two's complement)
+  bool in = true;
 #pragma unroll
   for (int k = 1; k < 9; ++k) {
-    const float t = fminf(fmaxf(fmaf(h[k], I16_IQ, I16_MAGIC), I16_MAGIC - 32768.0f), I16_MAGIC + 32767.0f);
+    const float r = fmaf(h[k], iq, I16_MAGIC);
+    in = in && (r >= I16_LO) && (r <= I16_HI);
+    const float t = fminf(fmaxf(r, I16_LO), I16_HI);
     b[k] = __float_as_uint(t);
     s += b[k] - mb;
   }
   // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is exact
-  const int n0 = (int)(__float_as_uint(fmaf(d, I16_IQ, I16_MAGIC)) - mb) - (int)s;
+  const int n0 = (int)(__float_as_uint(fmaf(d, iq, I16_MAGIC)) - mb) - (int)s;
   b[0] = (unsigned)min(max(n0, -32768), 32767);
+  return !(in && n0 >= -32768 && n0 <= 32767);
 }
 
 // The general (unshifted) path holds f = n Q + w rounded to FP32; the nearest
 // step of f - w recovers n exactly (the FP32 rounding is far below Q / 2).
 // i16_mass: a node's stored sum from its unshifted values (exact), and
 // i16_store_node: the conserving quantisation of a node's post-collision f
-// as int16 step counts.
-__device__ __forceinline__ float i16_mass(const float (&f)[9], const float (&w)[9]) {
+// as int16 step counts (true when a value saturated or was not finite).
+__device__ __forceinline__ float i16_mass(const float (&f)[9], const float (&w)[9], float iq, float q) {
   float s = 0.0f;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) s += i16_steps(f[k] - w[k]);
-  return s * I16_Q;
+  for (int k = 0; k < 9; ++k) s += i16_steps(f[k] - w[k], iq);
+  return s * q;
 }
-__device__ __forceinline__ void i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
-                                               short (&out)[9]) {
+__device__ __forceinline__ bool i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
+                                               short (&out)[9], float iq) {
   float h[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) h[k] = f[k] - w[k];
   unsigned b[9];
-  i16_conserve_bits(h, mass, b);
+  const bool bad = i16_conserve_bits(h, mass, b, iq);
 #pragma unroll
   for (int k = 0; k < 9; ++k) out[k] = (short)(b[k] & 0xffffu);
+  return bad;
+}
+
+// a post-collision value that is not finite (NaN or infinite)
+__device__ __forceinline__ bool not_finite(float v) { return !(fabsf(v) <= 3.402823466e38f); }
+
+// record a status bit in the sticky status word, if the plan has one
+__device__ __forceinline__ void report_status(int32_t* status, int bit) {
+  if (status) atomicOr(status, bit);
 }
 
 template <int BYTES>
@@ -312,10 +355,10 @@ __device__ __forceinline__ void gather_node(const FusedParams& p, int x, int y, 
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     if (k > 0 && (code & (1u << (k - 1)))) {
-      g[k] = S::dec(load1(src + OPP(k) * p.plane + (size_t)y * p.pitch + x), p.wsh[OPP(k)]);
+      g[k] = S::dec(load1(src + OPP(k) * p.plane + (size_t)y * p.pitch + x), p.wsh[OPP(k)], p.fq);
     } else {
       const int xs = wrap(x - CX(k), p.nx), ys = wrap(y - CY(k), p.ny);
-      g[k] = S::dec(load1(src + k * p.plane + (size_t)ys * p.pitch + xs), p.wsh[k]);
+      g[k] = S::dec(load1(src + k * p.plane + (size_t)ys * p.pitch + xs), p.wsh[k], p.fq);
     }
   }
 }
@@ -533,7 +576,7 @@ __device__ __forceinline__ void gather_direct(const FusedParams& p, int y, int s
       T raw[V];
       load_vec<T, V>(row + x0, raw);
 #pragma unroll
-      for (int i = 0; i < V; ++i) c[i] = S::dec(raw[i], p.wsh[k]);
+      for (int i = 0; i < V; ++i) c[i] = S::dec(raw[i], p.wsh[k], p.fq);
     } else {
 #pragma unroll
       for (int i = 0; i < V; ++i) c[i] = 0.0f;
@@ -543,18 +586,18 @@ __device__ __forceinline__ void gather_direct(const FusedParams& p, int y, int s
       for (int i = 0; i < V; ++i) f[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0 && live) left = S::dec(load1(row + wrap(x0 - 1, p.nx)), p.wsh[k]);
+      if (lane == 0 && live) left = S::dec(load1(row + wrap(x0 - 1, p.nx)), p.wsh[k], p.fq);
       f[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) f[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31 && live) right = S::dec(load1(row + wrap(x0 + V, p.nx)), p.wsh[k]);
+      if (lane == 31 && live) right = S::dec(load1(row + wrap(x0 + V, p.nx)), p.wsh[k], p.fq);
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) f[i][k] = c[i + 1];
       f[V - 1][k] = right;
       if (live && ilast < V) {  // node nx-1 pulls from column 0
-        const float v0 = S::dec(load1(row), p.wsh[k]);
+        const float v0 = S::dec(load1(row), p.wsh[k], p.fq);
 #pragma unroll
         for (int i = 0; i < V; ++i)
           if (i == ilast) f[i][k] = v0;
@@ -594,7 +637,7 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
 #pragma unroll
         for (int k = 1; k < 9; ++k)
           if (code[i] & (1u << (k - 1)))
-            f[i][k] = S::dec(load1(src + (size_t)OPP(k) * p.plane + rowoff + x0 + i), p.wsh[OPP(k)]);
+            f[i][k] = S::dec(load1(src + (size_t)OPP(k) * p.plane + rowoff + x0 + i), p.wsh[OPP(k)], p.fq);
       }
       const unsigned prog = code[i] >> LBM_CODE_PROG_SHIFT;
       if (prog) {
@@ -628,7 +671,7 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     float* fi = f[i];
-    if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh);
+    if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh, p.fiq, p.fq);
     const float rho = ((fi[0] + fi[1]) + (fi[2] + fi[3])) + ((fi[4] + fi[5]) + (fi[6] + fi[7])) + fi[8];
     const float jx = (fi[1] - fi[3]) + (fi[5] - fi[6]) + (fi[8] - fi[7]);
     const float jy = (fi[2] - fi[4]) + (fi[5] + fi[6]) - (fi[7] + fi[8]);
@@ -640,13 +683,17 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
       p.mom_out[2 * p.plane + q] = uy;
     }
     const float st = relax_collide<MODEL, PL, FORCE>(p, fi, rho, ux, uy, Fx, Fy, PL ? tau[i] : 0.0f);
+    // a node with a boundary program rounds its populations to nearest (its
+    // target sum is that of the rounded values): see i16_conserve_bits
+    if constexpr (ST == LBM_STORE_I16S)
+      if (code[i] >> LBM_CODE_PROG_SHIFT) mass[i] = i16_mass(f[i], p.wsh, p.fiq, p.fq);
     if (!(code[i] & LBM_CODE_ACTIVE)) {
       // not in the collision group: its post-collision populations never
       // change (the reference never writes f2 there), so carry them over
       if (live) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), p.wsh[k]);
-        if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh);
+        for (int k = 0; k < 9; ++k) fi[k] = S::dec(load1(src + (size_t)k * p.plane + rowoff + x0 + i), p.wsh[k], p.fq);
+        if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh, p.fiq, p.fq);
       }
     } else if (PL) {
       tau[i] = st;
@@ -657,8 +704,13 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   T* dst = reinterpret_cast<T*>(p.dst);
   if constexpr (ST == LBM_STORE_I16S) {
     short q[V][9];
+    bool bad = false;
 #pragma unroll
-    for (int i = 0; i < V; ++i) i16_store_node(f[i], p.wsh, mass[i], q[i]);
+    for (int i = 0; i < V; ++i) {
+      const bool b = i16_store_node(f[i], p.wsh, mass[i], q[i], p.fiq);
+      bad = bad || (b && (code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx);
+    }
+    if (bad) report_status(p.status, LBM_STATUS_SATURATED);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       T raw[V];
@@ -668,11 +720,15 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
     }
     return;
   }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < V; ++i) bad = bad || ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx && not_finite(f[i][0]));
+  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     T raw[V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], p.wsh[k]);
+    for (int i = 0; i < V; ++i) raw[i] = S::enc(f[i][k], p.wsh[k], p.fiq);
     store_vec<T, V>(dst + (size_t)k * p.plane + rowoff + x0, raw);
   }
 }
@@ -707,7 +763,7 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
       apply_bc<ST>(p, bi, x, y, f);
     }
     float mass = 0.0f;  // fixed-point storage: the node's stored sum before the collision
-    if constexpr (ST == LBM_STORE_I16S) mass = i16_mass(f, p.wsh);
+    if constexpr (ST == LBM_STORE_I16S) mass = i16_mass(f, p.wsh, p.fiq, p.fq);
     const float rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
     const float jx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
     const float jy = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
@@ -719,14 +775,19 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
     }
     const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
     if (PL) p.tau[q] = st;
+    // a node with a boundary program rounds its populations to nearest (see
+    // i16_conserve_bits)
+    if constexpr (ST == LBM_STORE_I16S)
+      if (prog) mass = i16_mass(f, p.wsh, p.fiq, p.fq);
     if constexpr (ST == LBM_STORE_I16S) {
       short n[9];
-      i16_store_node(f, p.wsh, mass, n);
+      if (i16_store_node(f, p.wsh, mass, n, p.fiq)) report_status(p.status, LBM_STATUS_SATURATED);
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = n[k];
     } else {
+      if (not_finite(f[0])) report_status(p.status, LBM_STATUS_NONFINITE);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k]);
+      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k], p.fiq);
     }
   }
 }
@@ -771,8 +832,8 @@ __global__ void k_convert(const FusedParams p, const float* in, void* out, int t
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const int k = (int)(t / p.plane);
     const float w = p.wsh[k];
-    if (to_storage) reinterpret_cast<T*>(out)[t] = S::enc(in[t], w);
-    else reinterpret_cast<float*>(out)[t] = S::dec(reinterpret_cast<const T*>(p.src)[t], w);
+    if (to_storage) reinterpret_cast<T*>(out)[t] = S::enc(in[t], w, p.fiq);
+    else reinterpret_cast<float*>(out)[t] = S::dec(reinterpret_cast<const T*>(p.src)[t], w, p.fq);
   }
 }
 
@@ -793,7 +854,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_momentum_exchange(const FusedParams
   for (int64_t m = threadIdx.x; m < n; m += blockDim.x) {
     const int64_t q = links[2 * m];
     const int k = links[2 * m + 1];
-    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
+    const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k], p.fq);
     fx += 2.0 * cx_dyn(k) * v;
     fy += 2.0 * cy_dyn(k) * v;
   }
@@ -812,6 +873,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_momentum_exchange(const FusedParams
     double s = 0.0;
     for (int i = 0; i < MEX_TPB / 32; ++i) s += sh[threadIdx.x][i];
     out[threadIdx.x] = s;
+    if (!(fabs(s) <= 1.7976931348623157e308)) report_status(p.status, LBM_STATUS_NONFINITE);
   }
 }
 
@@ -837,7 +899,7 @@ __global__ void __launch_bounds__(REDUCE_TPB) k_reduce_partial(const FusedParams
     if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
+      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k], p.fq);
       a0 += v;
       if (CX(k)) a1 += CX(k) * v;
       if (CY(k)) a2 += CY(k) * v;

@@ -12,9 +12,10 @@
 // k_fused_prefetch: each warp loops over its segments and issues the next
 // segment's vector loads into registers before colliding the current one.
 //
-// Every wait on an mbarrier is bounded by a clock64 budget; on expiry the
-// warp records LBM_STATUS_TIMEOUT in *status, waits (bounded again) for the
-// copies it still has in flight, and returns.
+// Every wait on an mbarrier is bounded by a clock64 budget (the plan's
+// wait_cycles, default WAIT_CYCLES); on expiry the warp records
+// LBM_STATUS_TIMEOUT in *status, waits (bounded by WAIT_CYCLES) for the
+// copies it still has in flight, the expired one included, and returns.
 #pragma once
 
 #include "lbm_fused.cuh"
@@ -56,13 +57,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; false when the budget ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false when the budget (clock cycles) ran out.  The first
+// test does not block, so a budget shorter than a copy's flight time runs
+// out before the copy lands (the short-budget test of the timeout path).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long budget) {
   const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > WAIT_CYCLES) return false;
+  if (mbar_test_wait(bar, parity)) return true;
+  while (clock64() - t0 <= budget) {
+    if (mbar_try_wait(bar, parity)) return true;
   }
-  return true;
+  return false;
 }
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile(
@@ -78,7 +91,6 @@ __device__ __forceinline__ void fence_mbarrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-#define LBM_STATUS_TIMEOUT 1
 
 // Fix-ups of the gather at the lattice's x edges: node 0 pulls column nx-1
 // on links with cx = +1, node nx-1 pulls column 0 on links with cx = -1.
@@ -94,9 +106,9 @@ __device__ __forceinline__ void edge_fixups(const FusedParams& p, float (&f)[AV]
 #pragma unroll
   for (int k = 1; k < 9; ++k) {
     const T* grow = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
-    if (CX(k) == 1 && first) f[0][k] = S::dec(load1(grow + (p.nx - 1)), p.wsh[k]);
+    if (CX(k) == 1 && first) f[0][k] = S::dec(load1(grow + (p.nx - 1)), p.wsh[k], p.fq);
     if (CX(k) == -1 && last) {
-      const float v0 = S::dec(load1(grow), p.wsh[k]);
+      const float v0 = S::dec(load1(grow), p.wsh[k], p.fq);
 #pragma unroll
       for (int i = 0; i < AV; ++i)
         if (i == ilast) f[i][k] = v0;
@@ -154,12 +166,13 @@ __global__ void __launch_bounds__(NW * 32) k_fused_async(const FusedParams p, in
     if (it >= nitems) break;
     issue(n + NS - 1);
     const int slot = (int)(n % NS);
-    const bool ok = mbar_wait_bounded(&bars[slot], (uint32_t)((n / NS) & 1));
+    const bool ok = mbar_wait_bounded(&bars[slot], (uint32_t)((n / NS) & 1), p.wait_cycles);
     if (!__all_sync(0xffffffffu, ok)) {
-      if (lane == 0) atomicExch(status, LBM_STATUS_TIMEOUT);
-      // drain: the copies issued for segments n + 1 .. n + NS - 1
-      for (long long m = n + 1; m < n + NS; ++m)
-        if (gw + m * GW < nitems) mbar_wait_bounded(&bars[m % NS], (uint32_t)((m / NS) & 1));
+      if (lane == 0) atomicOr(status, LBM_STATUS_TIMEOUT);
+      // drain, with the long budget: the copies still in flight, issued for
+      // segments n .. n + NS - 1, land before the warp leaves its ring
+      for (long long m = n; m < n + NS; ++m)
+        if (gw + m * GW < nitems) mbar_wait_bounded(&bars[m % NS], (uint32_t)((m / NS) & 1), WAIT_CYCLES);
       return;
     }
     const int y = (int)(it / p.nseg), seg = (int)(it - (long long)y * p.nseg);
@@ -171,7 +184,7 @@ __global__ void __launch_bounds__(NW * 32) k_fused_async(const FusedParams p, in
     for (int k = 0; k < 9; ++k) {
       const T* r = stage + k * G::ROW + G::PADE + lane * AV - CX(k);
 #pragma unroll
-      for (int i = 0; i < AV; ++i) f[i][k] = S::dec(r[i], p.wsh[k]);
+      for (int i = 0; i < AV; ++i) f[i][k] = S::dec(r[i], p.wsh[k], p.fq);
     }
     __syncwarp();
     edge_fixups<ST>(p, f, y, x0, live);
@@ -227,20 +240,20 @@ __global__ void __launch_bounds__(256) k_fused_prefetch(const FusedParams p) {
     for (int k = 0; k < 9; ++k) {
       float c[AV];
 #pragma unroll
-      for (int i = 0; i < AV; ++i) c[i] = live ? S::dec(cur.v[k][i], p.wsh[k]) : 0.0f;
+      for (int i = 0; i < AV; ++i) c[i] = live ? S::dec(cur.v[k][i], p.wsh[k], p.fq) : 0.0f;
       if (CX(k) == 0) {
 #pragma unroll
         for (int i = 0; i < AV; ++i) f[i][k] = c[i];
       } else if (CX(k) == 1) {
         float left = __shfl_up_sync(FULL, c[AV - 1], 1);
-        if (lane == 0 && live) left = S::dec(cur.left[li], p.wsh[k]);
+        if (lane == 0 && live) left = S::dec(cur.left[li], p.wsh[k], p.fq);
         ++li;
         f[0][k] = left;
 #pragma unroll
         for (int i = 1; i < AV; ++i) f[i][k] = c[i - 1];
       } else {
         float right = __shfl_down_sync(FULL, c[0], 1);
-        if (lane == 31 && live) right = S::dec(cur.right[ri], p.wsh[k]);
+        if (lane == 31 && live) right = S::dec(cur.right[ri], p.wsh[k], p.fq);
         ++ri;
 #pragma unroll
         for (int i = 0; i < AV - 1; ++i) f[i][k] = c[i + 1];
@@ -255,7 +268,7 @@ __global__ void __launch_bounds__(256) k_fused_prefetch(const FusedParams p) {
 #pragma unroll
       for (int k = 1; k < 9; ++k)
         if (CX(k) == -1) {
-          const float v0 = S::dec(load1(src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch), p.wsh[k]);
+          const float v0 = S::dec(load1(src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch), p.wsh[k], p.fq);
 #pragma unroll
           for (int i = 0; i < AV; ++i)
             if (i == ilast) f[i][k] = v0;

@@ -17,30 +17,44 @@
 namespace lbm {
 
 // ------------------------------------------------------------ raw conversion
+// The fixed-point step of a plan, as the raw conversions use it: q = 2^-e,
+// off = (2^23 + 2^15) q, iq = 1 / q (other storages ignore it).
+struct Fix {
+  float q, off, iq;
+};
+template <class P>
+__device__ __forceinline__ Fix fix_of(const P& p) {
+  return Fix{p.fq, p.foff, p.fiq};
+}
+
 template <int ST>
-__device__ __forceinline__ float raw_to_float(typename Storage<ST>::T v);
+__device__ __forceinline__ float raw_to_float(typename Storage<ST>::T v, const Fix& fx);
 template <>
-__device__ __forceinline__ float raw_to_float<LBM_STORE_F32>(float v) { return v; }
+__device__ __forceinline__ float raw_to_float<LBM_STORE_F32>(float v, const Fix&) { return v; }
 template <>
-__device__ __forceinline__ float raw_to_float<LBM_STORE_F16S>(__half v) { return __half2float(v); }
+__device__ __forceinline__ float raw_to_float<LBM_STORE_F16S>(__half v, const Fix&) { return __half2float(v); }
 template <>
-__device__ __forceinline__ float raw_to_float<LBM_STORE_BF16S>(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float raw_to_float<LBM_STORE_BF16S>(__nv_bfloat16 v, const Fix&) {
+  return __bfloat162float(v);
+}
 template <>
-__device__ __forceinline__ float raw_to_float<LBM_STORE_I16S>(short v) { return (float)v * I16_Q; }
+__device__ __forceinline__ float raw_to_float<LBM_STORE_I16S>(short v, const Fix& fx) { return (float)v * fx.q; }
 
 // two int16 step counts packed in a word -> their shifted values, without
 // an integer conversion: 0x4B00xxxx with xxxx = n + 2^15 is the float
 // 2^23 + 2^15 + n, and (that - 2^23 - 2^15) * Q is n * Q, exact in one fma
-__device__ __forceinline__ float2 i16_pair_to_floats(unsigned w) {
+// (Q is a power of two)
+__device__ __forceinline__ float2 i16_pair_to_floats(unsigned w, const Fix& fx) {
   const unsigned u = w ^ 0x80008000u;
   const float lo = __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7610));
   const float hi = __uint_as_float(__byte_perm(u, 0x4B000000u, 0x7632));
-  return make_float2(fmaf(lo, I16_Q, -16.0625f), fmaf(hi, I16_Q, -16.0625f));
+  return make_float2(fmaf(lo, fx.q, -fx.off), fmaf(hi, fx.q, -fx.off));
 }
 
 // V stored values -> floats (no shift)
 template <int ST, int V>
-__device__ __forceinline__ void raw_to_floats(const typename Storage<ST>::T (&raw)[V], float (&c)[V]) {
+__device__ __forceinline__ void raw_to_floats(const typename Storage<ST>::T (&raw)[V], float (&c)[V],
+                                              const Fix& fx) {
   if constexpr (ST == LBM_STORE_F32) {
 #pragma unroll
     for (int i = 0; i < V; ++i) c[i] = raw[i];
@@ -67,7 +81,7 @@ __device__ __forceinline__ void raw_to_floats(const typename Storage<ST>::T (&ra
     for (int i = 0; i < V; i += 2) {
       unsigned w;
       memcpy(&w, &raw[i], sizeof(w));
-      const float2 u = i16_pair_to_floats(w);
+      const float2 u = i16_pair_to_floats(w, fx);
       c[i] = u.x;
       c[i + 1] = u.y;
     }
@@ -122,16 +136,16 @@ __device__ __forceinline__ T load1_early(const T* p) {
 
 // V consecutive stored values -> floats (no shift)
 template <int ST, int V>
-__device__ __forceinline__ void load_raw(const typename Storage<ST>::T* p, float (&c)[V]) {
+__device__ __forceinline__ void load_raw(const typename Storage<ST>::T* p, float (&c)[V], const Fix& fx) {
   using T = typename Storage<ST>::T;
   T raw[V];
   load_vec_early<T, V>(p, raw);
-  raw_to_floats<ST, V>(raw, c);
+  raw_to_floats<ST, V>(raw, c, fx);
 }
 
 // V floats -> V consecutive stored values (round to nearest, no shift)
 template <int ST, int V>
-__device__ __forceinline__ void store_raw(typename Storage<ST>::T* p, const float (&c)[V]) {
+__device__ __forceinline__ void store_raw(typename Storage<ST>::T* p, const float (&c)[V], const Fix& fx) {
   using T = typename Storage<ST>::T;
   T raw[V];
   if constexpr (ST == LBM_STORE_F32) {
@@ -152,7 +166,7 @@ __device__ __forceinline__ void store_raw(typename Storage<ST>::T* p, const floa
   } else {
 #pragma unroll
     for (int i = 0; i < V; i += 2) {
-      const unsigned w = __byte_perm(i16_bits(i16_steps(c[i])), i16_bits(i16_steps(c[i + 1])), 0x5410);
+      const unsigned w = __byte_perm(i16_bits(i16_steps(c[i], fx.iq)), i16_bits(i16_steps(c[i + 1], fx.iq)), 0x5410);
       memcpy(&raw[i], &w, sizeof(w));
     }
   }
@@ -173,19 +187,19 @@ __device__ __forceinline__ void gather_interior(const P& p, int y, int x0, int l
     const int ys = CY(k) == 0 ? y : (CY(k) == 1 ? ym : yp);
     const T* row = src + (size_t)k * p.plane + (size_t)ys * p.pitch + x0;
     float c[V];
-    load_raw<ST, V>(row, c);
+    load_raw<ST, V>(row, c, fix_of(p));
     if (CX(k) == 0) {
 #pragma unroll
       for (int i = 0; i < V; ++i) h[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0) left = raw_to_float<ST>(load1_early(row - 1));
+      if (lane == 0) left = raw_to_float<ST>(load1_early(row - 1), fix_of(p));
       h[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31) right = raw_to_float<ST>(load1_early(row + V));
+      if (lane == 31) right = raw_to_float<ST>(load1_early(row + V), fix_of(p));
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];
       h[V - 1][k] = right;
@@ -207,7 +221,7 @@ __device__ __forceinline__ void gather_edge(const P& p, int y, int x0, int lane,
     const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
     float c[V];
     if (live) {
-      load_raw<ST, V>(row + x0, c);
+      load_raw<ST, V>(row + x0, c, fix_of(p));
     } else {
 #pragma unroll
       for (int i = 0; i < V; ++i) c[i] = 0.0f;
@@ -217,18 +231,18 @@ __device__ __forceinline__ void gather_edge(const P& p, int y, int x0, int lane,
       for (int i = 0; i < V; ++i) h[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0 && live) left = raw_to_float<ST>(load1_early(row + wrap(x0 - 1, p.nx)));
+      if (lane == 0 && live) left = raw_to_float<ST>(load1_early(row + wrap(x0 - 1, p.nx)), fix_of(p));
       h[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
-      if (lane == 31 && live) right = raw_to_float<ST>(load1_early(row + wrap(x0 + V, p.nx)));
+      if (lane == 31 && live) right = raw_to_float<ST>(load1_early(row + wrap(x0 + V, p.nx)), fix_of(p));
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];
       h[V - 1][k] = right;
       if (live && ilast < V) {  // node nx-1 pulls from column 0
-        const float v0 = raw_to_float<ST>(load1_early(row));
+        const float v0 = raw_to_float<ST>(load1_early(row), fix_of(p));
 #pragma unroll
         for (int i = 0; i < V; ++i)
           if (i == ilast) h[i][k] = v0;
@@ -465,12 +479,18 @@ __device__ __forceinline__ float node_sum(const float (&h)[9]) {
 // Fixed-point storage: quantise V nodes' post-collision values h with each
 // node's pre-collision mass kept (i16_conserve_bits) and store the nine
 // planes from p (population k at p + k * plane), two step counts per word.
+// Returns true when a value of one of the first nv nodes (the ones inside
+// the lattice; the rest is row padding) saturated or was not finite.
 template <int V>
-__device__ __forceinline__ void store_i16_conserved(short* p, size_t plane, const float (&h)[V][9],
-                                                    const float (&mass)[V]) {
+__device__ __forceinline__ bool store_i16_conserved(short* p, size_t plane, const float (&h)[V][9],
+                                                    const float (&mass)[V], float iq, int nv) {
   unsigned b[V][9];
+  bool bad = false;
 #pragma unroll
-  for (int i = 0; i < V; ++i) i16_conserve_bits(h[i], mass[i], b[i]);
+  for (int i = 0; i < V; ++i) {
+    const bool out = i16_conserve_bits(h[i], mass[i], b[i], iq);
+    bad = bad || (out && i < nv);
+  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     short raw[V];
@@ -481,6 +501,7 @@ __device__ __forceinline__ void store_i16_conserved(short* p, size_t plane, cons
     }
     store_vec<short, V>(p + (size_t)k * plane, raw);
   }
+  return bad;
 }
 
 // Moments, collision and stores of one lane's V nodes (x0.., row y) of a
@@ -513,15 +534,20 @@ __device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9],
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
   if constexpr (ST == LBM_STORE_I16S) {
-    store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass);
+    if (store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass, p.fiq, p.nx - x0))
+      report_status(p.status, LBM_STATUS_SATURATED);
     return;
   }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < V; ++i) bad = bad || (x0 + i < p.nx && not_finite(h[i][0]));
+  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     float c[V];
 #pragma unroll
     for (int i = 0; i < V; ++i) c[i] = h[i][k];
-    store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, c);
+    store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, c, fix_of(p));
   }
 }
 
@@ -605,14 +631,14 @@ __device__ __forceinline__ const void* edge_word(const typename Storage<ST>::T* 
   return ST == LBM_STORE_F32 ? (const void*)(row + x) : (const void*)(row + (x & ~1));
 }
 template <int ST>
-__device__ __forceinline__ float edge_value(uint32_t w, int x) {
+__device__ __forceinline__ float edge_value(uint32_t w, int x, const Fix& fx) {
   if constexpr (ST == LBM_STORE_F32) {
     return __uint_as_float(w);
   } else {
     const unsigned short b = (unsigned short)((x & 1) ? (w >> 16) : (w & 0xffffu));
     typename Storage<ST>::T t;
     memcpy(&t, &b, 2);
-    return raw_to_float<ST>(t);
+    return raw_to_float<ST>(t, fx);
   }
 }
 
@@ -661,7 +687,7 @@ __device__ __forceinline__ void stage_gather_row(const P& p, const unsigned char
     if (live) {
       T raw[V];
       memcpy(raw, stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), sizeof(raw));
-      raw_to_floats<ST, V>(raw, c);
+      raw_to_floats<ST, V>(raw, c, fix_of(p));
     } else {
 #pragma unroll
       for (int i = 0; i < V; ++i) c[i] = 0.0f;
@@ -671,14 +697,14 @@ __device__ __forceinline__ void stage_gather_row(const P& p, const unsigned char
       for (int i = 0; i < V; ++i) h[i][k] = c[i];
     } else if (CX(k) == 1) {
       float left = __shfl_up_sync(FULL, c[V - 1], 1);
-      if (lane == 0 && live) left = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xl);
+      if (lane == 0 && live) left = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xl, fix_of(p));
       h[0][k] = left;
 #pragma unroll
       for (int i = 1; i < V; ++i) h[i][k] = c[i - 1];
     } else {
       float right = __shfl_down_sync(FULL, c[0], 1);
       float re = 0.0f;
-      if ((lane == 31 || has_last) && live) re = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xr);
+      if ((lane == 31 || has_last) && live) re = edge_value<ST>(edges[edge_slot(k) * 32 + lane], xr, fix_of(p));
       if (lane == 31) right = re;
 #pragma unroll
       for (int i = 0; i < V - 1; ++i) h[i][k] = c[i + 1];

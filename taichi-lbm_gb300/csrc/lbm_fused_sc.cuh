@@ -70,7 +70,8 @@ __device__ __forceinline__ float density_at(const P& p, int x, int y) {
 #pragma unroll
   for (int k = 0; k < 9; ++k)
     h[k] = raw_to_float<ST>(load1_early(src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch +
-                                        wrap(x - CX(k), p.nx)));
+                                        wrap(x - CX(k), p.nx)),
+                            fix_of(p));
   return density_raw(h, p.rho_shift);
 }
 
@@ -153,7 +154,7 @@ __device__ __forceinline__ void sc_stage_psi(const P& p, unsigned char* st, int 
   }
   int k;
   const int xs = sc_halo_column<P, V>(p, x0s, lane, k);
-  const float v = xs >= 0 ? edge_value<ST>(reinterpret_cast<const uint32_t*>(st + G::ITEM_OFF)[lane], xs) : 0.0f;
+  const float v = xs >= 0 ? edge_value<ST>(reinterpret_cast<const uint32_t*>(st + G::ITEM_OFF)[lane], xs, fix_of(p)) : 0.0f;
   const float a = v + __shfl_down_sync(FULL, v, 1);  // (h0+h1) (h2+h3) (h4+h5) (h6+h7) at k = 0, 2, 4, 6
   const float b = a + __shfl_down_sync(FULL, a, 2);  // at k = 0, 4
   const float c = b + __shfl_down_sync(FULL, b, 4);  // at k = 0
@@ -210,13 +211,17 @@ __device__ __forceinline__ void sc_stage_collide(const P& p, const unsigned char
     T raw[V];
     memcpy(raw, st + k * ScGeom<ST, V>::POP_BYTES + lane * V * (int)sizeof(T), sizeof(raw));
     float c[V];
-    raw_to_floats<ST, V>(raw, c);
+    raw_to_floats<ST, V>(raw, c, fix_of(p));
 #pragma unroll
     for (int i = 0; i < V; ++i) h[i][k] = c[i];
   }
 #pragma unroll
   for (int i = 0; i < V; ++i) collide_lean<P, MODEL, false, 2>(p, h[i], 0.0f, Fx[i], Fy[i]);
   if (x0 >= p.nx) return;
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < V; ++i) bad = bad || (x0 + i < p.nx && not_finite(h[i][0]));
+  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
   T* dst = reinterpret_cast<T*>(p.dst);
   const size_t rowoff = (size_t)y * p.pitch;
 #pragma unroll
@@ -224,7 +229,7 @@ __device__ __forceinline__ void sc_stage_collide(const P& p, const unsigned char
     float v[V];
 #pragma unroll
     for (int i = 0; i < V; ++i) v[i] = h[i][k];
-    store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, v);
+    store_raw<ST, V>(dst + (size_t)k * p.plane + rowoff + x0, v, fix_of(p));
   }
 }
 

@@ -1,4 +1,5 @@
 // Fused-step plans: validation, buffer binding and stream-ordered launches.
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -29,6 +30,7 @@ FusedParams params_for(const LbmPlan* pl) {
   p.code = pl->b.code;
   p.seg_flags = pl->b.seg_flags;
   p.tau = pl->b.tau;
+  p.status = pl->b.status;
   // two-pass forms: direct (special list), prefetch (special and plain lists)
   const bool two = !pl->d.sc && pl->b.special &&
                    (pl->d.pipeline == LBM_PIPE_DIRECT || (pl->d.pipeline == LBM_PIPE_PREFETCH && pl->b.plain));
@@ -151,7 +153,11 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   if (d->pipeline != LBM_PIPE_DIRECT && V != lbm::AV && !(d->pipeline == LBM_PIPE_PREFETCH && V == 8))
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "persistent pipelines run %d nodes per thread (prefetch: also 8 "
                         "with 16-bit storage)", lbm::AV);
-  if (d->sc && d->storage == LBM_STORE_I16S)  // phase separation leaves the +-1/16 range of the steps
+  if (d->fixed_exp != 0 && (d->fixed_exp < LBM_FIXED_EXP_MIN || d->fixed_exp > LBM_FIXED_EXP_MAX))
+    return lbm_err::set(LBM_ERR_ARG, "fixed_exp %d outside [%d, %d]", d->fixed_exp, LBM_FIXED_EXP_MIN,
+                        LBM_FIXED_EXP_MAX);
+  if (d->wait_cycles < 0) return lbm_err::set(LBM_ERR_ARG, "wait_cycles %lld", (long long)d->wait_cycles);
+  if (d->sc && d->storage == LBM_STORE_I16S)  // the strips' stores do not conserve a node's stored sum
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans store fp32, fp16 or bf16 populations");
   if (d->pipeline == LBM_PIPE_ASYNC && d->storage == LBM_STORE_I16S)
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "the fixed-point storage runs the direct or prefetch pipeline");
@@ -211,6 +217,11 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   p.sc_T = d->sc_T;
   p.eos = d->eos;
   p.tune = d->tune;
+  const int e = d->fixed_exp ? d->fixed_exp : LBM_FIXED_EXP_DEFAULT;
+  p.fq = std::ldexp(1.0f, -e);
+  p.fiq = std::ldexp(1.0f, e);
+  p.foff = std::ldexp(1.0f, 23 - e) + std::ldexp(1.0f, 15 - e);
+  p.wait_cycles = d->wait_cycles ? (long long)d->wait_cycles : lbm::WAIT_CYCLES;
   if (!(d->rho_ref >= 0.0f && d->rho_ref < 1e30f))
     return lbm_err::set(LBM_ERR_ARG, "rho_ref %g must be finite and >= 0", (double)d->rho_ref);
   const float rho_ref = d->rho_ref != 0.0f ? d->rho_ref : 1.0f;
@@ -429,7 +440,7 @@ __global__ void __launch_bounds__(lbm::REDUCE_TPB) k_reduce_chunked(const FusedP
     if (x >= p.nx || !(p.code[q] & LBM_CODE_ACTIVE)) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k]);
+      const double v = S::dec64(src[(size_t)k * p.plane + q], p.wsh[k], p.fq);
       a0 += v;
       if (lbm::CX(k)) a1 += lbm::CX(k) * v;
       if (lbm::CY(k)) a2 += lbm::CY(k) * v;

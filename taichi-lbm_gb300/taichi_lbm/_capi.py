@@ -70,8 +70,14 @@ class LbmPlanDesc(ctypes.Structure):
                 ("nprog", ctypes.c_int32), ("prog", (ctypes.c_int8 * PROG_LEN) * MAX_PROG),
                 ("pipeline", ctypes.c_int32), ("tune", ctypes.c_int32),
                 ("sc", ctypes.c_int32), ("g_coh", ctypes.c_float), ("sc_T", ctypes.c_float),
-                ("eos", LbmEos), ("rho_ref", ctypes.c_float)]
+                ("eos", LbmEos), ("rho_ref", ctypes.c_float), ("fixed_exp", ctypes.c_int32),
+                ("wait_cycles", ctypes.c_int64)]
 
+
+# fixed-point storage step 2^-fixed_exp (range 2^(15 - fixed_exp))
+FIXED_EXP_DEFAULT, FIXED_EXP_MIN, FIXED_EXP_MAX = 19, 12, 22
+# sticky bits of a plan's device status word
+STATUS_TIMEOUT, STATUS_SATURATED, STATUS_NONFINITE = 1, 2, 4
 
 PIPE_DIRECT, PIPE_ASYNC, PIPE_PREFETCH = 0, 1, 2
 ASYNC_TUNINGS = 4

@@ -18,9 +18,19 @@ Each result is the same as running the request alone (FusedSolver.step with
 forces), because a batch computes every member with the single-lattice
 arithmetic (see Batch).  Latency is completion minus arrival, in seconds of
 the server's clock.
+
+Failure detection: every member plan has a device status word that its
+kernels set when a colliding node's populations turn NaN or infinite, when
+the fixed-point storage saturates, or when its drag/lift monitor sums to a
+non-finite force.  After each slice the members' words are copied to pinned
+host memory behind the slice's event; once that event has completed, a
+member with a bit set is evicted at the next slice boundary (it leaves the
+batch and is retired with ``failed`` set), and its lattice updates are not
+counted in the aggregate.  The other members are not touched.
 """
 import collections
 import time
+import warnings
 
 import numpy as np
 import torch
@@ -45,6 +55,9 @@ class Request:
         self.fields = None      # optional final fields (keep_fields)
         self.finite = None
         self.updated_nodes = None
+        self.updates = 0        # lattice updates run for this request
+        self.failed = None      # status bits that evicted it (diverged), else None
+        self.steps_run = 0
 
     @property
     def nodes(self):
@@ -147,14 +160,27 @@ class Server:
             _, series, count = mon
             n = min(int(count.item()), series.shape[0])
             req.forces = series[:n].cpu().numpy()
-            solver.finish()
-            req.finite = bool(torch.isfinite(solver.lb._rho).all())
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")  # a diverged member's finish() warns; its status says so
+                solver.finish()
+            if req.failed is None and solver.status_bits:
+                req.failed = solver.status_bits
+            req.finite = bool(torch.isfinite(solver.lb._rho).all()) and req.failed is None
             if self.keep_fields:
                 req.fields = {"rho": solver.lb.rho.to_numpy(), "vel": solver.lb.vel.to_numpy()}
             self.retire_stream.synchronize()
         req.finished = now_fn()
         self.used -= nbytes
         self.done.append(req)
+
+    def _check(self, slots, host):
+        """Status words of a completed slice (pinned host copy): members
+        with a bit set are marked for eviction."""
+        for slot, bits in zip(slots, host.tolist()):
+            a = self.active.get(slot)
+            if bits and a is not None and a[0].failed is None:
+                a[0].failed = int(bits)
+                a[2] = 0  # leaves at the next slice boundary
 
     def _leave(self, retiring):
         """Members at zero remaining steps leave the batch (no wait); their
@@ -220,16 +246,25 @@ class Server:
                     # at most `ahead` slices queued: the scheduler (and the
                     # builders' small GPU steps) stay close to the GPU's clock
                     while len(inflight) >= self.ahead:
-                        inflight.popleft().synchronize()
+                        ev0, slots0, host0 = inflight.popleft()
+                        ev0.synchronize()
+                        self._check(slots0, host0)
+                    self._leave(retiring)  # evicted members leave before the next slice
+                if self.active:
                     k = min(self.slice_steps, min(a[2] for a in self.active.values()))
                     self.batch.run(k)
+                    # the members' status words, copied behind the slice
+                    slots = list(self.active)
+                    host = torch.empty(len(slots), dtype=torch.int32, pin_memory=True)
+                    host.copy_(torch.stack([self.active[sl][1].status[0] for sl in slots]), non_blocking=True)
                     ev = torch.cuda.Event()
                     ev.record()
-                    inflight.append(ev)
+                    inflight.append((ev, slots, host))
                     launched = True
                     for a in self.active.values():
                         a[2] -= k
-                        self.lattice_updates += k * a[0].updated_nodes
+                        a[0].updates += k * a[0].updated_nodes
+                        a[0].steps_run += k
                 # retire what finished in earlier slices while this one runs
                 for entry in retiring:
                     self._retire(entry, now)
@@ -240,8 +275,12 @@ class Server:
                     building[0][1].result()
                 elif pending:
                     time.sleep(max(0.0, min(pending[0].arrival - now(), 0.001)))
+        for ev0, slots0, host0 in inflight:
+            ev0.synchronize()
         for r in self.done:
-            self.lattice_updates += r.updated_nodes  # the staged first step of each request
+            r.updates += r.updated_nodes  # the staged first step of each request
+            if r.failed is None:  # evicted (diverged) requests' work is not counted
+                self.lattice_updates += r.updates
         return self.done
 
     def close(self):
@@ -283,4 +322,5 @@ def summarize(done, makespan, lattice_updates):
             "MLUPS": round(lattice_updates / makespan / 1e6, 1),
             "p50_s": round(float(np.percentile(lat, 50)), 4), "p99_s": round(float(np.percentile(lat, 99)), 4),
             "finite": int(sum(1 for r in done if r.finite)),
-            "nonfinite_requests": sorted(int(r.rid) for r in done if not r.finite)}
+            "nonfinite_requests": sorted(int(r.rid) for r in done if not r.finite),
+            "evicted_requests": sorted(int(r.rid) for r in done if r.failed is not None)}

@@ -28,8 +28,8 @@ from .boundary import BoundaryCondition
 from .collision import BGKCollision, MRTCollision, PowerLawFluid, TRTCollision
 from .lbm import stream_handle
 
-# "i16s": int16 fixed point (steps of 2^-19) of f - w_k rho_ref; every
-# collision conserves each node's stored mass exactly
+# "i16s": int16 fixed point (steps of 2^-fixed_exp, default 2^-19) of
+# f - w_k rho_ref; every collision conserves each node's stored mass exactly
 STORAGE = {"fp32": A.STORE_F32, "fp16s": A.STORE_F16S, "bf16s": A.STORE_BF16S, "i16s": A.STORE_I16S}
 DEFAULT_V = {A.STORE_F32: 4, A.STORE_F16S: 4, A.STORE_BF16S: 4, A.STORE_I16S: 4}
 STATE_DTYPE = {A.STORE_F16S: torch.float16, A.STORE_BF16S: torch.bfloat16, A.STORE_I16S: torch.int16}
@@ -52,8 +52,13 @@ def boundary_items(boundary_engine):
 class FusedSolver:
     def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
                  nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
-                 sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True, lane_special=True):
+                 sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True, lane_special=True,
+                 fixed_exp=None, wait_cycles=0):
         self.sc = lb_field.sc_field
+        # fixed-point storage: step 2^-fixed_exp, range |f - w rho_ref| < 2^(15 - fixed_exp)
+        self.fixed_exp = int(fixed_exp) if fixed_exp is not None else A.FIXED_EXP_DEFAULT
+        self.wait_cycles = int(wait_cycles)
+        self.status_bits = 0
         self.lane_special = bool(lane_special)
         self.two_pass = bool(two_pass)
         self.overlap = bool(overlap)
@@ -199,6 +204,8 @@ class FusedSolver:
             for s in range(A.PROG_LEN):
                 d.prog[p][s] = int(cp.programs[p, s])
         d.rho_ref = self._rho_ref()
+        d.fixed_exp = self.fixed_exp
+        d.wait_cycles = self.wait_cycles
         self.desc = d
         # flagged segments, listed for the two-pass direct step
         flags = np.asarray(cp.seg_flags).ravel()
@@ -297,18 +304,40 @@ class FusedSolver:
         """nsteps fused steps on the current state (no staging)."""
         A.call("lbm_plan_run", self._plan, int(nsteps), stream_handle())
 
+    @property
+    def saturated(self):
+        """The fixed-point storage clamped a colliding node's value (or met a
+        non-finite one) during the last run: set from the device status word
+        at finish()."""
+        return bool(self.status_bits & A.STATUS_SATURATED)
+
+    @property
+    def nonfinite(self):
+        """A colliding node's post-collision value was NaN or infinite during
+        the last run (floating-point storages), read at finish()."""
+        return bool(self.status_bits & A.STATUS_NONFINITE)
+
+    def read_status(self):
+        """The device status word's sticky LBM_STATUS_* bits of the current run
+        (synchronises with the current stream)."""
+        return int(self.status.item())
+
     def finish(self):
         """Last stream/boundary pass and moment prologue; f, f2, rho, vel current."""
         lb = self.lb
         lb._fused_owner = None
         self._live = False
-        if self.pipeline == A.PIPE_ASYNC and int(self.status.item()) != 0:
-            self.status.zero_()
+        self.status_bits = self.read_status()
+        self.status.zero_()
+        if self.status_bits & A.STATUS_TIMEOUT:
             raise A.LbmError("fused step: a wait on a shared-memory copy exceeded its time budget; "
                              "the state is invalid")
         par = ctypes.c_int32()
         A.call("lbm_plan_get_parity", self._plan, ctypes.byref(par))
         s = stream_handle()
+        if self.nonfinite:
+            warnings.warn("fused run: a colliding node's populations became NaN or infinite (the flow "
+                          "diverged)")
         if self.fbuf is None:
             if par.value == 0:  # state in f2 -> write f
                 A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
@@ -316,13 +345,11 @@ class FusedSolver:
                 A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
                 lb._f, lb._f2 = lb._f2, lb._f
         else:
-            if self.storage == A.STORE_I16S:
-                # the fixed-point steps saturate at +-2^15 (|f - w rho_ref| >= 1/16)
-                st = self.fbuf[par.value]
-                self.saturated = int(torch.count_nonzero((st == 32767) | (st == -32768)).item())
-                if self.saturated:
-                    warnings.warn(f"fixed-point storage saturated at {self.saturated} stored values "
-                                  "(|f - w rho_ref| >= 1/16); use fp32 or fp16s for this flow")
+            if self.storage == A.STORE_I16S and self.saturated:
+                rng = 2.0 ** (15 - self.fixed_exp)
+                warnings.warn(f"fixed-point storage saturated: a colliding node left |f - w rho_ref| < "
+                              f"{rng:g} (fixed_exp={self.fixed_exp}); use a smaller fixed_exp, or fp32 or "
+                              "fp16s, for this flow")
             A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
             A.call("lbm_plan_export", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
         if self.powerlaw:

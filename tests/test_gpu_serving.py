@@ -1,7 +1,10 @@
 """GPU tests of the serving loop: requests that arrive while others run are
 admitted into the running batch (continuous batching) within an HBM budget,
 and every request's result (final fields and its drag/lift series) is the
-same as running it alone through FusedSolver.step(n, forces=True)."""
+same as running it alone through FusedSolver.step(n, forces=True).  A
+request that diverges (here: one whose initial populations hold a NaN,
+planted on the host) is evicted at a slice boundary without touching the
+others, and its work is not counted."""
 import numpy as np
 import pytest
 
@@ -67,3 +70,41 @@ def test_admission_respects_budget(tl):
         assert b.admitted >= a.finished - 1e-9
     with pytest.raises(ValueError):
         server.submit(tl.Request(9, 2048, 512, "bgk", 0.6, 10, storage="fp32"))
+
+
+def poisoned_request(tl, *a, **kw):
+    """A Request whose lattice starts with a NaN in one fluid node's
+    populations (host-side fault injection: the run diverges at once)."""
+    class Poisoned(tl.Request):
+        def build(self, tl_, keep_init=False, nodes_per_thread=None):
+            s = super().build(tl_, keep_init=keep_init, nodes_per_thread=nodes_per_thread)
+            s.lb._f[1, self.ny // 2, self.nx // 2 + self.nx // 4] = float("nan")
+            return s
+    return Poisoned(*a, **kw)
+
+
+@pytest.mark.parametrize("storage", ["fp16s", "i16s"])
+def test_diverged_request_is_evicted(tl, storage):
+    server = tl.Server(tl, hbm_budget=8 << 30, graphs=True, slice_steps=16, keep_fields=True)
+    good = [tl.Request(0, 256, 64, "bgk", 0.56, 600, arrival=0.0, storage=storage),
+            tl.Request(2, 192, 48, "trt", 0.6, 300, arrival=0.0, storage=storage)]
+    bad = poisoned_request(tl, 1, 160, 40, "mrt", 0.58, 5000, arrival=0.0, storage=storage)
+    for r in (good[0], bad, good[1]):
+        server.submit(r)
+    done = {r.rid: r for r in server.run()}
+    server.close()
+    assert sorted(done) == [0, 1, 2]
+    b = done[1]
+    assert b.failed and not b.finite
+    assert b.steps_run < b.steps  # left the batch long before its step count
+    for r in good:
+        g = done[r.rid]
+        assert g.failed is None and g.finite
+        alone = tl.Request(r.rid, r.nx, r.ny, r.model, r.tau, r.steps, storage=storage)
+        s = alone.build(tl)
+        series = s.step(r.steps, forces=True).cpu().numpy()
+        for k, ref in (("rho", s.lb.rho.to_numpy()), ("vel", s.lb.vel.to_numpy())):
+            assert rel_err(g.fields[k], ref) <= 1e-3, (r.rid, k)
+        assert np.abs(g.forces - series).max() <= 1e-3 * max(np.abs(series).max(), 1e-12)
+    # only the finished requests' updates are counted
+    assert server.lattice_updates == sum(r.updates for r in done.values() if r.failed is None)

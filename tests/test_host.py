@@ -23,7 +23,7 @@ def test_library_exports_every_header_function(built):
     for n in names:
         assert hasattr(lib, n), f"{n} declared in lbm_gb300.h but not exported"
     assert set(names) == set(_capi.EXPORTED)
-    assert lib.lbm_abi_version() == 2
+    assert lib.lbm_abi_version() == 3
 
 
 def test_library_reports_argument_errors(built):
