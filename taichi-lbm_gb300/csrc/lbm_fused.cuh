@@ -230,13 +230,14 @@ struct Storage<LBM_STORE_I16S> {
 // for the fixed-point storage: populations 1..8 round to their nearest
 // step, and population 0 takes the rest of the node's pre-collision mass
 // d (a sum of stored values, exact), so the stored sum equals d exactly.
-// Colliding nodes without a boundary program conserve so; so a closed
+// Colliding nodes without a boundary program conserve so, and a closed
 // lattice keeps its mass to the bit.  A node whose populations a boundary
-// program rewrote passes the sum of its rounded post-collision values as d
-// instead (plain rounding to nearest): its boundary sets the mass that
-// crosses it, and conserving the rounded boundary values there biases the
-// mass an open channel carries, step after step, when its outlet does not
-// pin the density (PressureNEEM writes rho_value to total_rho only).
+// program rewrote holds values that are not multiples of Q; its d is the
+// node's post-boundary mass rounded once to the nearest step
+// (i16_mass_rounded), not the sum of its nine values each rounded: that sum
+// carries up to 4.5 steps of rounding per node and step, which an open
+// channel whose outlet does not pin the density (PressureNEEM writes
+// rho_value to total_rho only) accumulates as a drift of its mass.
 // h: shifted post-collision values; iq = 1 / Q.  b[k]: the int16 bits of the
 // stored step counts in the low half of each word.  The rounding yields
 // t = n + 1.5 * 2^23 as a float, whose bit pattern is that of 1.5 * 2^23
@@ -271,6 +272,14 @@ __device__ __forceinline__ float i16_mass(const float (&f)[9], const float (&w)[
 #pragma unroll
   for (int k = 0; k < 9; ++k) s += i16_steps(f[k] - w[k], iq);
   return s * q;
+}
+// a boundary node's post-boundary mass, summed in float and rounded once
+// to the nearest step
+__device__ __forceinline__ float i16_mass_rounded(const float (&f)[9], const float (&w)[9], float iq, float q) {
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s += f[k] - w[k];
+  return (fmaf(s, iq, I16_MAGIC) - I16_MAGIC) * q;
 }
 __device__ __forceinline__ bool i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
                                                short (&out)[9], float iq) {
@@ -671,7 +680,9 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
 #pragma unroll
   for (int i = 0; i < V; ++i) {
     float* fi = f[i];
-    if constexpr (ST == LBM_STORE_I16S) mass[i] = i16_mass(f[i], p.wsh, p.fiq, p.fq);
+    if constexpr (ST == LBM_STORE_I16S)
+      mass[i] = (code[i] >> LBM_CODE_PROG_SHIFT) ? i16_mass_rounded(f[i], p.wsh, p.fiq, p.fq)
+                                                 : i16_mass(f[i], p.wsh, p.fiq, p.fq);
     const float rho = ((fi[0] + fi[1]) + (fi[2] + fi[3])) + ((fi[4] + fi[5]) + (fi[6] + fi[7])) + fi[8];
     const float jx = (fi[1] - fi[3]) + (fi[5] - fi[6]) + (fi[8] - fi[7]);
     const float jy = (fi[2] - fi[4]) + (fi[5] + fi[6]) - (fi[7] + fi[8]);
@@ -683,10 +694,6 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
       p.mom_out[2 * p.plane + q] = uy;
     }
     const float st = relax_collide<MODEL, PL, FORCE>(p, fi, rho, ux, uy, Fx, Fy, PL ? tau[i] : 0.0f);
-    // a node with a boundary program rounds its populations to nearest (its
-    // target sum is that of the rounded values): see i16_conserve_bits
-    if constexpr (ST == LBM_STORE_I16S)
-      if (code[i] >> LBM_CODE_PROG_SHIFT) mass[i] = i16_mass(f[i], p.wsh, p.fiq, p.fq);
     if (!(code[i] & LBM_CODE_ACTIVE)) {
       // not in the collision group: its post-collision populations never
       // change (the reference never writes f2 there), so carry them over
@@ -763,7 +770,8 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
       apply_bc<ST>(p, bi, x, y, f);
     }
     float mass = 0.0f;  // fixed-point storage: the node's stored sum before the collision
-    if constexpr (ST == LBM_STORE_I16S) mass = i16_mass(f, p.wsh, p.fiq, p.fq);
+    if constexpr (ST == LBM_STORE_I16S)
+      mass = prog ? i16_mass_rounded(f, p.wsh, p.fiq, p.fq) : i16_mass(f, p.wsh, p.fiq, p.fq);
     const float rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
     const float jx = (f[1] - f[3]) + (f[5] - f[6]) + (f[8] - f[7]);
     const float jy = (f[2] - f[4]) + (f[5] + f[6]) - (f[7] + f[8]);
@@ -775,10 +783,7 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
     }
     const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
     if (PL) p.tau[q] = st;
-    // a node with a boundary program rounds its populations to nearest (see
-    // i16_conserve_bits)
-    if constexpr (ST == LBM_STORE_I16S)
-      if (prog) mass = i16_mass(f, p.wsh, p.fiq, p.fq);
+
     if constexpr (ST == LBM_STORE_I16S) {
       short n[9];
       if (i16_store_node(f, p.wsh, mass, n, p.fiq)) report_status(p.status, LBM_STATUS_SATURATED);

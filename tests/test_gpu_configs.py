@@ -14,9 +14,11 @@ the floor is printed beside the result.
 
 The roofline lattice, 8192 x 2048 (disc r = 200 at (1600, 1024), u_max =
 0.04, tau = 0.52), under BGK, TRT (magic 1/4) and MRT (s = [0, 1.64, 1.54,
-0, 1.7, 0, 1.7, 1/tau, 1/tau]): the whole lattice against the fp32 oracle
-for LBM_CONFIG2_STEPS steps (default 100; the oracle needs 16.8 M node
-updates per step on the host cores).  Bound 1e-5 of each field's maximum.
+0, 1.7, 0, 1.7, 1/tau, 1/tau]): the whole lattice against the oracle in
+single and double precision for LBM_CONFIG2_STEPS steps (default 100; the
+oracle needs 16.8 M node updates per step on the host cores).  The fp32 path
+must be at least as accurate as the reference's own fp32 arithmetic:
+distance from the double run <= 1.5 x the single run's distance + 1e-6.
 """
 import json
 import os
@@ -64,7 +66,8 @@ def test_cylinder_400x100_10000_steps(tl):
     err = {k: rel_err(got[k], ref64[k]) for k in ("rho", "vel")}
     floor = {k: rel_err(ref32[k], ref64[k]) for k in ("rho", "vel")}
     ferr = float(np.abs(series - ser64).max() / np.abs(ser64).max())
-    print(json.dumps({"case": "cylinder 400x100", "steps": steps, "rel_err_rho": err["rho"],
+    print(json.dumps({"case": "cylinder 400x100", "steps": steps, "where_vel": where_max(got["vel"], ref64["vel"]),
+                      "rel_err_rho": err["rho"],
                       "rel_err_vel": err["vel"], "oracle_fp32_floor_rho": floor["rho"],
                       "oracle_fp32_floor_vel": floor["vel"], "drag_lift_rel_err": ferr,
                       "drag_final": float(series[-1, 0]), "lift_final": float(series[-1, 1])}))
@@ -73,6 +76,14 @@ def test_cylinder_400x100_10000_steps(tl):
         assert err[k] <= 2e-4, (k, err, floor)
     assert ferr <= 1e-3
     assert series[-1, 0] > 0  # drag points downstream
+
+
+def where_max(a, b):
+    """(i, j) of the largest difference of two fields (max over components)."""
+    d = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    if d.ndim == 3:
+        d = d.max(-1)
+    return [int(v) for v in np.unravel_index(np.argmax(d), d.shape)]
 
 
 @pytest.mark.parametrize("model", ["bgk", "trt", "mrt"])
@@ -85,11 +96,18 @@ def test_roofline_lattice_8192x2048(tl, model):
     meta, arrays = describe(lb, coll, be, steps)
     s = tl.FusedSolver(lb, me, coll, be)
     s.step(steps)
-    got = fields_of(lb)
+    got = {k: v for k, v in fields_of(lb).items() if k in ("rho", "vel")}
     del lb, me, coll, be, s
-    ref = O.replay(meta, arrays)
-    err = {k: rel_err(got[k], ref[k]) for k in ("rho", "vel")}
-    print(json.dumps({"case": "cylinder 8192x2048", "model": model, "steps": steps,
-                      "rel_err_rho": err["rho"], "rel_err_vel": err["vel"]}))
+    ref32 = O.replay(meta, arrays)
+    ref32 = {k: ref32[k] for k in ("rho", "vel")}
+    a64 = {k: (v.astype(np.float64) if v.dtype == np.float32 else v) for k, v in arrays.items()}
+    ref64 = O.replay(dict(meta, fp="f64"), a64)
+    e32 = {k: rel_err(got[k], ref32[k]) for k in ("rho", "vel")}
+    e64 = {k: rel_err(got[k], ref64[k]) for k in ("rho", "vel")}
+    floor = {k: rel_err(ref32[k], ref64[k]) for k in ("rho", "vel")}
+    print(json.dumps({"case": "cylinder 8192x2048", "model": model, "steps": steps, "vs_fp32_oracle": e32,
+                      "vs_fp64_oracle": e64, "oracle_fp32_floor": floor,
+                      "where_vel_vs_fp32": where_max(got["vel"], ref32["vel"]),
+                      "where_vel_vs_fp64": where_max(got["vel"], ref64["vel"])}))
     for k in ("rho", "vel"):
-        assert err[k] <= 1e-5, (k, err)
+        assert e64[k] <= 1.5 * floor[k] + 1e-6, (k, e32, e64, floor)
