@@ -62,8 +62,14 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--requests", type=int, default=64, help="requests in the served stream")
     ap.add_argument("--mix-only", type=int, default=0, metavar="N",
-                    help="only time the batched step of the first N served requests (fp16s, all packed)")
+                    help="only time the batched step of the first N served requests (all packed)")
     ap.add_argument("--mix-v", type=int, default=None, help="nodes per thread of the --mix-only members")
+    ap.add_argument("--mix-storage", default="i16s", choices=["fp16s", "bf16s", "i16s"],
+                    help="storage of the --mix-only members")
+    ap.add_argument("--served-storage", default="i16s", choices=["fp32", "fp16s", "bf16s", "i16s"],
+                    help="storage of the served requests")
+    ap.add_argument("--batched-only", default=None, choices=["fp32", "fp16s", "bf16s"], metavar="STORAGE",
+                    help="time only the batched Shan-Chen lattices in this storage")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -461,8 +467,9 @@ def run_ours(a):
                          "2048}, NY = NX/4, r = NY/10 at x = NX/5, Re ~ U[20, 200] via tau (u_max 0.04), "
                          "steps log-uniform in [2000, 50000], BGK/TRT/MRT uniform, 20% power law n ~ "
                          "U[0.5, 1.5]; Poisson arrivals at 80% of the capacity implied by the single-lattice "
-                         "BGK fp16s MLUPS; fp16s storage, HBM budget 64 GiB, 200-step slices, CUDA graphs"},
-            **run_served(tl, a.requests, cap, local))
+                         f"BGK fp16s MLUPS; {a.served_storage} storage, HBM budget 64 GiB, 200-step slices, "
+                         "CUDA graphs; diverged requests are evicted and their updates not counted"},
+            **run_served(tl, a.requests, cap, local, storage=a.served_storage))
     if rank == 0 and ws == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(cfg, a.model, a.cpu_seconds)
     if dist is not None:
@@ -531,12 +538,12 @@ def run_reference(a):
 
 def run_mix(a):
     """The batched step of a served mix on its own: the first N requests of
-    the seeded served stream (fp16s), all in the packed tile table, direct
+    the seeded served stream (storage --mix-storage), all in the packed tile table, direct
     launches (no graph), K timed steps after W warm-up steps."""
     import torch
     import taichi_lbm as tl
     from taichi_lbm.serving import request_stream
-    reqs = request_stream(a.mix_only, 20.0)
+    reqs = request_stream(a.mix_only, 20.0, storage=a.mix_storage)
     solvers = [r.build(tl, nodes_per_thread=a.mix_v) for r in reqs]
     nodes = sum(s.coll.group.n for s in solvers)
     batch = tl.Batch(graphs=False, solo_nodes=0)
@@ -554,7 +561,7 @@ def run_mix(a):
     print(json.dumps({"metric": METRIC, "value": round(nodes / ms / 1e3, 1), "unit": METRIC, "steps": a.steps,
                       "warmup": a.warmup, "ms_per_step": round(ms, 4), "nodes": nodes, "info": batch.info(),
                       "config": {"workload": f"batched step of the first {a.mix_only} served requests (seed "
-                                             "20261203), fp16s, every member packed, direct launches",
+                                             f"20261203), {a.mix_storage}, every member packed, direct launches",
                                  "nodes_per_thread": solvers[0].V}}))
     batch.close()
 
@@ -563,6 +570,9 @@ def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.batched_only:
+        import taichi_lbm as tl
+        print(json.dumps({"batched": run_batched(tl, a.batched_only, a.steps, max(3, a.warmup), 0)}))
     elif a.mix_only:
         run_mix(a)
     else:
