@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--mix-only", type=int, default=0, metavar="N",
                     help="only time the batched step of the first N served requests (all packed)")
     ap.add_argument("--mix-v", type=int, default=None, help="nodes per thread of the --mix-only members")
+    ap.add_argument("--mix-form", type=int, default=0, choices=[0, 1, 2],
+                    help="lean kernel form of the --mix-only batch (lbm_batch_set_lean_form)")
     ap.add_argument("--mix-storage", default="i16s", choices=["fp16s", "bf16s", "i16s"],
                     help="storage of the --mix-only members")
     ap.add_argument("--served-storage", default="i16s", choices=["fp32", "fp16s", "bf16s", "i16s"],
@@ -546,7 +548,7 @@ def run_mix(a):
     reqs = request_stream(a.mix_only, 20.0, storage=a.mix_storage)
     solvers = [r.build(tl, nodes_per_thread=a.mix_v) for r in reqs]
     nodes = sum(s.coll.group.n for s in solvers)
-    batch = tl.Batch(graphs=False, solo_nodes=0)
+    batch = tl.Batch(graphs=False, solo_nodes=0, lean_form=a.mix_form)
     for s in solvers:
         batch.add(s)
     batch.run(a.warmup)
@@ -562,7 +564,7 @@ def run_mix(a):
                       "warmup": a.warmup, "ms_per_step": round(ms, 4), "nodes": nodes, "info": batch.info(),
                       "config": {"workload": f"batched step of the first {a.mix_only} served requests (seed "
                                              f"20261203), {a.mix_storage}, every member packed, direct launches",
-                                 "nodes_per_thread": solvers[0].V}}))
+                                 "nodes_per_thread": solvers[0].V, "lean_form": a.mix_form}}))
     batch.close()
 
 

@@ -460,6 +460,13 @@ int lbm_batch_set_solo(LbmBatch* batch, int64_t min_nodes);
  * by rows): 8, 16 or 32, or 0 for the default (the longest strips that
  * still give every SM several). */
 int lbm_batch_set_sc_rows(LbmBatch* batch, int32_t rows);
+/* Kernel form of the plain-segment (lean) groups: 0 = one pass per tile, 16
+ * tiles per block; 1 = a two-stage cp.async ring per warp, 32 tiles per
+ * block; 2 = a three-stage ring, 64 tiles per block.  The pipelined forms
+ * keep the next tiles' rows in flight while a warp collides the current one;
+ * every form gives the same results to the bit.  Takes effect at the next
+ * run (the tables are rebuilt). */
+int lbm_batch_set_lean_form(LbmBatch* batch, int32_t form);
 int lbm_batch_run(LbmBatch* batch, int32_t nsteps, void* stream);
 /* members; tiles and launch units (tile groups and solo members) of the
  * current tables (-1 before the first run after a change) */

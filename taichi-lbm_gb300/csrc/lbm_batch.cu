@@ -82,6 +82,8 @@ struct LbmBatch {
   int64_t solo_nodes = int64_t(1) << 19;
   // rows per Shan-Chen strip (8, 16 or 32); 0 chooses from the batch's size
   int sc_rows_fixed = 0;
+  // form of the lean groups (0: k_batch_lean; 1, 2: k_batch_lean_pf)
+  int lean_form = 0;
   struct Solo {
     int storage, V, flip;
     lbm::FusedParams p[2];  // [parity]
@@ -310,7 +312,8 @@ int rebuild(LbmBatch* b) {
         for (int l = 0; l < 32; ++l)
           if (mk >> l & 1u) ts.push_back({lat, item * 32 + l});
       }
-      while (tl.size() % (lbm::BATCH_WARPS * lbm::BATCH_TPW)) tl.push_back({lat, -1});  // whole blocks per lattice
+      // whole blocks per lattice
+      while (tl.size() % lbm::lean_block_tiles(b->lean_form)) tl.push_back({lat, -1});
     }
     if (m.monitored) {
       BatchMonitor bm;
@@ -337,6 +340,7 @@ int rebuild(LbmBatch* b) {
     g.storage = e.first.storage;
     g.V = e.first.V;
     g.force = e.first.force;
+    g.form = g.kind == lbm::BATCH_LEAN ? b->lean_form : 0;
     g.offset = (int)tiles.size();
     g.count = (int)e.second.size();
     g.blocks = 0;
@@ -515,6 +519,13 @@ int lbm_batch_remove(LbmBatch* b, int32_t slot) {
 int lbm_batch_set_solo(LbmBatch* b, int64_t min_nodes) {
   if (!b || min_nodes < 0) return lbm_err::set(LBM_ERR_ARG, "batch_set_solo: bad arguments");
   b->solo_nodes = min_nodes;
+  b->dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_set_lean_form(LbmBatch* b, int32_t form) {
+  if (!b || form < 0 || form > 2) return lbm_err::set(LBM_ERR_ARG, "batch_set_lean_form: form must be 0, 1 or 2");
+  b->lean_form = form;
   b->dirty = true;
   return LBM_OK;
 }

@@ -76,6 +76,92 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean(const BatchLatt
   }
 }
 
+// Pipelined form of k_batch_lean (batch lean forms 1 and 2).  A block serves
+// BATCH_WARPS * TPW tiles of one lattice; it stages the lattice's parameters
+// and its tile list in shared memory once.  Each warp walks its TPW tiles
+// (tile j * BATCH_WARPS + warp) through a ring of NS shared-memory stages:
+// the stage of a tile holds every lane's V elements of the nine pulled rows,
+// the words across the segment's edges (stage_issue_row) and the segment's
+// lane mask, all copied by cp.async, so the rows of the next NS - 1 tiles
+// are in flight while the warp collides the current one.  Each lane reads
+// back only what it copied itself (cp.async.wait_group is the hardware wait
+// for the lane's own copies; no barrier).  The gather and the collision are
+// the single-lattice kernels' own, so results are bit-identical to them.
+template <int ST, int V, int NS>
+struct BatchPfGeom {
+  using G = PfGeom<ST, V, NS>;
+  static constexpr int MASK_OFF = G::STAGE_BYTES;  // [32] copies of the segment's lane mask
+  static constexpr int STRIDE = G::STAGE_BYTES + 32 * 4;
+  static constexpr int WARP_BYTES = NS * STRIDE;
+  static constexpr int BLOCK_BYTES = BATCH_WARPS * WARP_BYTES;
+  static_assert(STRIDE % 16 == 0, "stages must stay 16-byte aligned");
+};
+
+// (ring stages, tiles per warp) of the pipelined lean forms
+template <int FORM>
+struct LeanForm;
+template <>
+struct LeanForm<1> {
+  static constexpr int NS = 2, TPW = 4;
+};
+template <>
+struct LeanForm<2> {
+  static constexpr int NS = 3, TPW = 8;
+};
+__host__ __device__ constexpr int lean_block_tiles(int form) {
+  return BATCH_WARPS * (form == 1 ? LeanForm<1>::TPW : form == 2 ? LeanForm<2>::TPW : BATCH_TPW);
+}
+
+template <bool PL, int ST, int V, int FORCE, int FORM>
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean_pf(const BatchLattice* __restrict__ lats,
+                                                                     const BatchTile* __restrict__ tiles,
+                                                                     int ntiles, int sp) {
+  constexpr int NS = LeanForm<FORM>::NS, TPW = LeanForm<FORM>::TPW;
+  using B = BatchPfGeom<ST, V, NS>;
+  __shared__ LeanParams p;
+  __shared__ int items[BATCH_WARPS * TPW];
+  extern __shared__ __align__(16) unsigned char lean_ring[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t0 = blockIdx.x * (BATCH_WARPS * TPW);
+  const int lat = tiles[t0].lat;
+  copy_words(&p, &lats[lat].lean[view_of(lats, lat, sp)], threadIdx.x, BATCH_WARPS * 32);
+  for (int i = threadIdx.x; i < BATCH_WARPS * TPW; i += BATCH_WARPS * 32) items[i] = tiles[t0 + i].item;
+  __syncthreads();
+  unsigned char* ring = lean_ring + warp * B::WARP_BYTES;
+  // stage the copies of the warp's tile j (none past the last) and commit them as one group
+  auto issue = [&](int j) {
+    const int item = j < TPW ? items[j * BATCH_WARPS + warp] : -1;
+    if (item >= 0) {
+      unsigned char* stage = ring + (j % NS) * B::STRIDE;
+      const int y = fast_div(item, p.nseg_mul, p.nseg_shift);
+      stage_issue_row<LeanParams, ST, V, NS>(p, stage, y, (item - y * p.nseg) * 32 * V, lane);
+      cp_async<4>(stage + B::MASK_OFF + lane * 4, p.lane_mask + item);
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < NS - 1; ++j) issue(j);
+#pragma unroll 1
+  for (int j = 0; j < TPW; ++j) {
+    issue(j + NS - 1);
+    cp_async_wait<NS - 1>();  // this lane's copies of tile j have landed
+    const int item = items[j * BATCH_WARPS + warp];
+    if (item < 0) continue;
+    const unsigned char* stage = ring + (j % NS) * B::STRIDE;
+    const uint32_t mask = reinterpret_cast<const uint32_t*>(stage + B::MASK_OFF)[lane];
+    if (mask == 0xffffffffu) continue;  // uniform over the warp
+    const int y = fast_div(item, p.nseg_mul, p.nseg_shift);
+    const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
+    float h[V][9];
+    stage_gather_row<LeanParams, ST, V, NS>(p, stage, x0, lane, h);
+    const bool skip = (mask >> lane) & 1u;
+    if (p.model == LBM_BGK) lean_collide_store<LeanParams, LBM_BGK, PL, ST, V, FORCE>(p, h, y, x0, skip);
+    else if (p.model == LBM_TRT) lean_collide_store<LeanParams, LBM_TRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+    else lean_collide_store<LeanParams, LBM_MRT, PL, ST, V, FORCE>(p, h, y, x0, skip);
+  }
+  cp_async_wait<0>();
+}
+
 // Marked lanes (bounce-back links, boundary programs, saved moments,
 // inactive nodes) of every lattice in the table, V threads per lane entry
 // ((y * nseg + seg) * 32 + lane), one per node: the general per-node path,
@@ -188,6 +274,7 @@ enum { BATCH_LEAN = 0, BATCH_SC = 1, BATCH_SPECIAL = 2 };  // launch order withi
 
 struct BatchGroup {
   int kind, model, powerlaw, storage, V, force;
+  int form;           // lean kinds: 0 = k_batch_lean, 1 / 2 = k_batch_lean_pf<FORM>
   int offset, count;  // range in the tile table
   int blocks;         // persistent grid (0 until first launch)
 };
@@ -207,6 +294,21 @@ int batch_grid(K kern, int threads, int tiles_per_block, int count, int* blocks)
   return need < *blocks ? need : *blocks;
 }
 
+template <int ST, int V, int FORM>
+int launch_batch_lean_pf(BatchGroup& g, const BatchLattice* lats, const BatchTile* t, int sp, cudaStream_t s) {
+  constexpr int smem = BatchPfGeom<ST, V, LeanForm<FORM>::NS>::BLOCK_BYTES;
+  auto kern = g.powerlaw ? (g.force ? k_batch_lean_pf<true, ST, V, 1, FORM> : k_batch_lean_pf<true, ST, V, 0, FORM>)
+                         : (g.force ? k_batch_lean_pf<false, ST, V, 1, FORM> : k_batch_lean_pf<false, ST, V, 0, FORM>);
+  if (smem > 48 * 1024) {
+    int rc = lbm_err::cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                           "batched step: shared-memory attribute");
+    if (rc) return rc;
+  }
+  constexpr int per = lean_block_tiles(FORM);
+  kern<<<(unsigned)((g.count + per - 1) / per), BATCH_WARPS * 32, smem, s>>>(lats, t, g.count, sp);
+  return lbm_err::launch("batched step (plain segments, pipelined)");
+}
+
 // groups of the segment kinds: lean groups per (power law, force), every
 // collision model in one launch; one marked-lane group for every model
 template <int ST, int V>
@@ -217,6 +319,8 @@ int launch_batch_v(BatchGroup& g, const BatchLattice* lats, const BatchTile* til
     k_batch_lanes<ST, V><<<(unsigned)(((long long)g.count * V + 127) / 128), 128, 0, s>>>(lats, t, g.count, sp);
     return lbm_err::launch("batched step (marked lanes)");
   }
+  if (g.form == 1) return launch_batch_lean_pf<ST, V, 1>(g, lats, t, sp, s);
+  if (g.form == 2) return launch_batch_lean_pf<ST, V, 2>(g, lats, t, sp, s);
   auto kern = g.powerlaw ? (g.force ? k_batch_lean<true, ST, V, 1> : k_batch_lean<true, ST, V, 0>)
                          : (g.force ? k_batch_lean<false, ST, V, 1> : k_batch_lean<false, ST, V, 0>);
   kern<<<(unsigned)((g.count + BATCH_WARPS * BATCH_TPW - 1) / (BATCH_WARPS * BATCH_TPW)), BATCH_WARPS * 32, 0, s>>>(

@@ -148,6 +148,7 @@ _SIGS = {
     "lbm_batch_set_graph": ([_vp, ctypes.c_int32], ctypes.c_int),
     "lbm_batch_set_solo": ([_vp, ctypes.c_int64], ctypes.c_int),
     "lbm_batch_set_sc_rows": ([_vp, ctypes.c_int32], ctypes.c_int),
+    "lbm_batch_set_lean_form": ([_vp, ctypes.c_int32], ctypes.c_int),
     "lbm_batch_run": ([_vp, ctypes.c_int32, _vp], ctypes.c_int),
     "lbm_batch_info": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "lbm_batch_destroy": ([_vp], ctypes.c_int),

@@ -7,7 +7,9 @@ shape the batch engine leaves open:
   for fp32 storage, 4 or 8 for the 16-bit shifted storages;
 * rows per Shan-Chen strip (8, 16, 32): the strip tile's height;
 * the solo threshold: members of at least that many nodes run their own
-  single-lattice step inside the batched step rather than the packed tiles.
+  single-lattice step inside the batched step rather than the packed tiles;
+* the kernel form of the packed plain segments (one pass per tile, or a
+  two- or three-stage cp.async pipeline per warp).
 
 Results are kept in a table keyed by what decides them (collision model,
 storage, power law, Shan-Chen, and the lattice's node count rounded to a
@@ -23,6 +25,7 @@ import torch
 V_CANDIDATES = {"fp32": (2, 4), "fp16s": (4, 8), "bf16s": (4, 8), "i16s": (4, 8)}
 SC_ROWS = (8, 16, 32)
 SOLO_CANDIDATES = (0, 1 << 18, 1 << 19, 1 << 20, 1 << 62)
+LEAN_FORMS = (0, 1, 2)
 
 
 def _elapsed_ms(fn, steps, warmup):
@@ -104,26 +107,29 @@ class Autotuner:
         or the default for V=None).  Each candidate is a new Batch over such
         members, timed over warmup + steps batched steps (the members'
         states advance; they are scratch).  Candidates: V over the storage's
-        pair (tune_v), and the strip rows (Shan-Chen) or solo thresholds."""
+        pair (tune_v), and the strip rows (Shan-Chen) or the solo thresholds
+        times the lean kernel forms.  The chosen lean form is kept in the
+        table entry (batch_kwargs passes it on)."""
         from .batch import Batch
         hit = self.table.get(key, {})
         if all(k in hit for k in ("V", "solo_nodes", "sc_rows")):
             return hit["V"], hit["solo_nodes"], hit["sc_rows"]
-        shapes = [(None, r) for r in SC_ROWS] if sc else [(n, None) for n in SOLO_CANDIDATES]
+        shapes = ([(None, r, None) for r in SC_ROWS] if sc
+                  else [(n, None, f) for n in SOLO_CANDIDATES for f in LEAN_FORMS])
         best, best_ms = None, None
         for V in (V_CANDIDATES[storage] if tune_v else (None,)):
             members = make_members(V)
-            for solo, rows in shapes:
-                b = Batch(graphs=graphs, solo_nodes=solo, sc_rows=rows)
+            for solo, rows, form in shapes:
+                b = Batch(graphs=graphs, solo_nodes=solo, sc_rows=rows, lean_form=form)
                 for s in members:
                     b.add(s)
                 ms = _elapsed_ms(b.run, self.steps, self.warmup)
                 for slot in list(b.members):
                     b.remove(slot)
                 b.close()
-                self.trials.append((key, {"V": V, "solo_nodes": solo, "sc_rows": rows}, ms))
+                self.trials.append((key, {"V": V, "solo_nodes": solo, "sc_rows": rows, "lean_form": form}, ms))
                 if best_ms is None or ms < best_ms:
-                    best, best_ms = (V, solo, rows), ms
+                    best, best_ms = (V, solo, rows, form), ms
             for s in members:
                 s.finish()
             del members
@@ -131,6 +137,7 @@ class Autotuner:
         ent["V"] = None if best[0] is None else int(best[0])
         ent["solo_nodes"] = -1 if best[1] is None else int(best[1])
         ent["sc_rows"] = 0 if best[2] is None else int(best[2])
+        ent["lean_form"] = 0 if best[3] is None else int(best[3])
         ent["batch_ms"] = best_ms
         return ent["V"], ent["solo_nodes"], ent["sc_rows"]
 
@@ -142,4 +149,6 @@ class Autotuner:
             kw["solo_nodes"] = int(ent["solo_nodes"])
         if ent.get("sc_rows", 0) > 0:
             kw["sc_rows"] = int(ent["sc_rows"])
+        if ent.get("lean_form", 0) > 0:
+            kw["lean_form"] = int(ent["lean_form"])
         return kw

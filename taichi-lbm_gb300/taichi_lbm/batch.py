@@ -22,11 +22,13 @@ from .lbm import stream_handle
 
 
 class Batch:
-    def __init__(self, graphs=True, solo_nodes=None, sc_rows=None):
+    def __init__(self, graphs=True, solo_nodes=None, sc_rows=None, lean_form=None):
         """solo_nodes: members of at least this many nodes run their own
         single-lattice step inside each batched step (lbm_batch_set_solo);
         None keeps the library default, 0 packs every member.  sc_rows: rows
-        per Shan-Chen strip (8, 16, 32; None chooses from the batch)."""
+        per Shan-Chen strip (8, 16, 32; None chooses from the batch).
+        lean_form: kernel form of the plain segments (lbm_batch_set_lean_form:
+        0 one pass per tile, 1 and 2 cp.async-pipelined; None keeps 0)."""
         h = ctypes.c_void_p()
         A.call("lbm_batch_create", ctypes.byref(h))
         self._h = h
@@ -36,6 +38,8 @@ class Batch:
             A.call("lbm_batch_set_solo", self._h, int(solo_nodes))
         if sc_rows is not None:
             A.call("lbm_batch_set_sc_rows", self._h, int(sc_rows))
+        if lean_form is not None:
+            A.call("lbm_batch_set_lean_form", self._h, int(lean_form))
         self.members = {}  # slot -> (solver, monitor tensors or None)
 
     @staticmethod

@@ -181,3 +181,27 @@ def test_batched_monitor_equals_plan_series(tl, solo):
     assert got.shape == ref.shape
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
     batch.close()
+
+
+@pytest.mark.parametrize("form", [1, 2])
+def test_lean_forms_equal_one_pass_form(tl, form):
+    """The cp.async-pipelined forms of the packed plain segments
+    (lbm_batch_set_lean_form 1 and 2) give every member the same populations
+    as the one-pass form, to the bit (the gather and the collision are the
+    same code; only where the source rows wait differs)."""
+    n = 30
+    kinds = [k for k in KINDS if not k.startswith("sc_")]
+    out = {}
+    for f in (0, form):
+        batch = tl.Batch(graphs=True, solo_nodes=0, lean_form=f)
+        solvers = {}
+        for k in kinds:
+            solvers[k] = make(tl, k)[0]()
+            batch.add(solvers[k])
+        batch.run(n - 1)
+        for k, s in solvers.items():
+            s.finish()
+            out[(f, k)] = fields_of(s.lb)["f"]
+        batch.close()
+    for k in kinds:
+        assert np.array_equal(out[(0, k)], out[(form, k)]), k
