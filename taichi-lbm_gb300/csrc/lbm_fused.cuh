@@ -247,19 +247,19 @@ struct Storage<LBM_STORE_I16S> {
 __device__ __forceinline__ bool i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9], float iq) {
   const unsigned mb = __float_as_uint(I16_MAGIC);
   unsigned s = 0u;  // sum of the steps of populations 1..8 (two's complement)
-  bool in = true;
+  bool out = false;
 #pragma unroll
   for (int k = 1; k < 9; ++k) {
     const float r = fmaf(h[k], iq, I16_MAGIC);
-    in = in && (r >= I16_LO) && (r <= I16_HI);
     const float t = fminf(fmaxf(r, I16_LO), I16_HI);
+    out = out || (t != r);  // clamped, or NaN (a NaN clamps to I16_LO)
     b[k] = __float_as_uint(t);
     s += b[k] - mb;
   }
   // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is exact
   const int n0 = (int)(__float_as_uint(fmaf(d, iq, I16_MAGIC)) - mb) - (int)s;
   b[0] = (unsigned)min(max(n0, -32768), 32767);
-  return !(in && n0 >= -32768 && n0 <= 32767);
+  return out || n0 < -32768 || n0 > 32767;
 }
 
 // The general (unshifted) path holds f = n Q + w rounded to FP32; the nearest
