@@ -306,8 +306,8 @@ enum { LBM_PIPE_DIRECT = 0, LBM_PIPE_ASYNC = 1, LBM_PIPE_PREFETCH = 2 };
  *                        value fell outside the fixed-point range (or was
  *                        not finite) and was clamped
  *  LBM_STATUS_NONFINITE  a colliding node's post-collision value was NaN or
- *                        infinite (floating-point storages), or a drag/lift
- *                        monitor summed to a non-finite force
+ *                        infinite (any storage), or a drag/lift monitor
+ *                        summed to a non-finite force
  * Only nodes inside the lattice whose code has LBM_CODE_ACTIVE are checked. */
 #define LBM_STATUS_TIMEOUT 1
 #define LBM_STATUS_SATURATED 2

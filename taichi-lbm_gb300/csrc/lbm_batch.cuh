@@ -263,8 +263,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_batch_monitor(const BatchLattice* _
     *m.count = c + 1;
     // a diverged member: its force is not finite (any NaN or infinity in
     // the summed links reaches the total)
-    if (!(fabs(sx) <= 1.7976931348623157e308 && fabs(sy) <= 1.7976931348623157e308))
-      report_status(p.status, LBM_STATUS_NONFINITE);
+    report_status(p.status, LBM_STATUS_NONFINITE, !(fabs(sx) <= 1.7976931348623157e308 && fabs(sy) <= 1.7976931348623157e308));
   }
 }
 

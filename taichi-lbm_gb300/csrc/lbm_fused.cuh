@@ -296,9 +296,18 @@ __device__ __forceinline__ bool i16_store_node(const float (&f)[9], const float 
 // a post-collision value that is not finite (NaN or infinite)
 __device__ __forceinline__ bool not_finite(float v) { return !(fabsf(v) <= 3.402823466e38f); }
 
-// record a status bit in the sticky status word, if the plan has one
-__device__ __forceinline__ void report_status(int32_t* status, int bit) {
-  if (status) atomicOr(status, bit);
+// Record a status bit in the sticky status word, if the plan has one, for
+// the lanes of the calling warp that pass bad.  One lane of the warp does
+// the atomic, and only when the bit is not yet set: a diverged lattice has
+// every node bad on every step, and an atomic per node and step on one word
+// would serialise the whole launch.
+__device__ __forceinline__ void report_status(int32_t* status, int bit, bool bad = true) {
+  const unsigned am = __activemask();
+  const unsigned any = __ballot_sync(am, bad);
+  if (!any || !status) return;
+  if ((int)(threadIdx.x & 31) == __ffs(any) - 1) {
+    if (!(*(volatile const int32_t*)status & bit)) atomicOr(status, bit);
+  }
 }
 
 template <int BYTES>
@@ -709,15 +718,19 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
+  bool bad = false;  // a colliding node inside the lattice holds NaN or infinity
+#pragma unroll
+  for (int i = 0; i < V; ++i) bad = bad || ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx && not_finite(f[i][0]));
+  report_status(p.status, LBM_STATUS_NONFINITE, bad);
   if constexpr (ST == LBM_STORE_I16S) {
     short q[V][9];
-    bool bad = false;
+    bool sat = false;
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       const bool b = i16_store_node(f[i], p.wsh, mass[i], q[i], p.fiq);
-      bad = bad || (b && (code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx);
+      sat = sat || (b && (code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx);
     }
-    if (bad) report_status(p.status, LBM_STATUS_SATURATED);
+    report_status(p.status, LBM_STATUS_SATURATED, sat);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       T raw[V];
@@ -727,10 +740,6 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
     }
     return;
   }
-  bool bad = false;
-#pragma unroll
-  for (int i = 0; i < V; ++i) bad = bad || ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx && not_finite(f[i][0]));
-  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     T raw[V];
@@ -784,13 +793,14 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
     const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
     if (PL) p.tau[q] = st;
 
+    report_status(p.status, LBM_STATUS_NONFINITE, not_finite(f[0]));
     if constexpr (ST == LBM_STORE_I16S) {
       short n[9];
-      if (i16_store_node(f, p.wsh, mass, n, p.fiq)) report_status(p.status, LBM_STATUS_SATURATED);
+      const bool sat = i16_store_node(f, p.wsh, mass, n, p.fiq);
+      report_status(p.status, LBM_STATUS_SATURATED, sat);
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = n[k];
     } else {
-      if (not_finite(f[0])) report_status(p.status, LBM_STATUS_NONFINITE);
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k], p.fiq);
     }
@@ -878,7 +888,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_momentum_exchange(const FusedParams
     double s = 0.0;
     for (int i = 0; i < MEX_TPB / 32; ++i) s += sh[threadIdx.x][i];
     out[threadIdx.x] = s;
-    if (!(fabs(s) <= 1.7976931348623157e308)) report_status(p.status, LBM_STATUS_NONFINITE);
+    report_status(p.status, LBM_STATUS_NONFINITE, !(fabs(s) <= 1.7976931348623157e308));
   }
 }
 

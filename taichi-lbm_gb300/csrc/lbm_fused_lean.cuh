@@ -533,15 +533,15 @@ __device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9],
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
-  if constexpr (ST == LBM_STORE_I16S) {
-    if (store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass, p.fiq, p.nx - x0))
-      report_status(p.status, LBM_STATUS_SATURATED);
-    return;
-  }
-  bool bad = false;
+  bool bad = false;  // a node inside the lattice holds NaN or infinity
 #pragma unroll
   for (int i = 0; i < V; ++i) bad = bad || (x0 + i < p.nx && not_finite(h[i][0]));
-  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
+  report_status(p.status, LBM_STATUS_NONFINITE, bad);
+  if constexpr (ST == LBM_STORE_I16S) {
+    const bool sat = store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass, p.fiq, p.nx - x0);
+    report_status(p.status, LBM_STATUS_SATURATED, sat);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     float c[V];

@@ -221,7 +221,7 @@ __device__ __forceinline__ void sc_stage_collide(const P& p, const unsigned char
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < V; ++i) bad = bad || (x0 + i < p.nx && not_finite(h[i][0]));
-  if (bad) report_status(p.status, LBM_STATUS_NONFINITE);
+  report_status(p.status, LBM_STATUS_NONFINITE, bad);
   T* dst = reinterpret_cast<T*>(p.dst);
   const size_t rowoff = (size_t)y * p.pitch;
 #pragma unroll

@@ -24,9 +24,15 @@ kernels set when a colliding node's populations turn NaN or infinite, when
 the fixed-point storage saturates, or when its drag/lift monitor sums to a
 non-finite force.  After each slice the members' words are copied to pinned
 host memory behind the slice's event; once that event has completed, a
-member with a bit set is evicted at the next slice boundary (it leaves the
-batch and is retired with ``failed`` set), and its lattice updates are not
-counted in the aggregate.  The other members are not touched.
+member with a bit set leaves the batch at the next slice boundary without
+touching the others.  A fixed-point member that only saturated (its flow
+left the storage's range, typically in the pressure transient of the
+impulsive start) is built again with a step twice as coarse (range twice as
+wide, down to fixed_exp 17) and queued ahead of new arrivals; its latency
+counts from its first arrival.  A member that turned non-finite, or still
+saturates at the coarsest step, is evicted (retired with ``failed`` set).
+The lattice updates of discarded attempts and of evicted requests are not
+counted in the aggregate.
 """
 import collections
 import time
@@ -35,6 +41,7 @@ import warnings
 import numpy as np
 import torch
 
+from . import _capi as A
 from .batch import Batch
 from .workloads import cylinder_channel
 
@@ -46,7 +53,7 @@ class Request:
     `steps` time steps, arriving at `arrival` seconds."""
 
     def __init__(self, rid, nx, ny, model, tau, steps, arrival=0.0, powerlaw=None, umax=0.04,
-                 storage="fp16s"):
+                 storage="fp16s", fixed_exp=None):
         self.rid, self.nx, self.ny = rid, int(nx), int(ny)
         self.model, self.tau, self.steps = model, float(tau), int(steps)
         self.arrival, self.powerlaw, self.umax, self.storage = float(arrival), powerlaw, umax, storage
@@ -58,6 +65,9 @@ class Request:
         self.updates = 0        # lattice updates run for this request
         self.failed = None      # status bits that evicted it (diverged), else None
         self.steps_run = 0
+        self.fixed_exp = fixed_exp  # fixed-point step 2^-fixed_exp (None: the default)
+        self.retries = 0        # rebuilds with a coarser fixed-point step
+        self.retry = False
 
     @property
     def nodes(self):
@@ -79,7 +89,8 @@ class Request:
         lb, me, coll, be = cylinder_channel(tl, self.nx, self.ny, r, self.nx / 5.0, self.ny / 2.0 - 0.5, self.tau,
                                             self.umax, model=self.model, mrt_s=s, keep_init=keep_init,
                                             name=f"req{self.rid}", powerlaw=self.powerlaw)
-        return tl.FusedSolver(lb, me, coll, be, storage=self.storage, nodes_per_thread=nodes_per_thread)
+        return tl.FusedSolver(lb, me, coll, be, storage=self.storage, nodes_per_thread=nodes_per_thread,
+                              fixed_exp=self.fixed_exp)
 
 
 def device_bytes(nx, ny, storage):
@@ -119,6 +130,8 @@ class Server:
         self.ahead = max(1, int(ahead))  # slices queued on the GPU before the scheduler waits
         self.reserve_bytes = int(reserve_bytes)
         self.queue = collections.deque()
+        self.requeue = []       # saturated fixed-point requests to build again
+        self.min_fixed_exp = 17
         self.active = {}        # slot -> [request, solver, remaining steps, bytes]
         self.done = []
         self.lattice_updates = 0
@@ -153,8 +166,21 @@ class Server:
 
     def _retire(self, entry, now_fn):
         """Finish a member that left the batch: on the retire stream, after
-        the event of the slice it finished in (later slices keep running)."""
+        the event of the slice it finished in (later slices keep running).
+        A member marked for a retry is dropped and queued again instead."""
         (req, solver, _, nbytes), mon, ev = entry
+        if req.retry:
+            with torch.cuda.stream(self.retire_stream):
+                self.retire_stream.wait_event(ev)
+                solver.status.zero_()
+                self.retire_stream.synchronize()
+            req.retry = False
+            req.retries += 1
+            req.fixed_exp = (req.fixed_exp or A.FIXED_EXP_DEFAULT) - 1
+            req.updates = req.steps_run = 0
+            self.used -= nbytes
+            self.requeue.append(req)
+            return
         with torch.cuda.stream(self.retire_stream):
             self.retire_stream.wait_event(ev)
             _, series, count = mon
@@ -175,12 +201,19 @@ class Server:
 
     def _check(self, slots, host):
         """Status words of a completed slice (pinned host copy): members
-        with a bit set are marked for eviction."""
+        with a bit set are marked to leave, for a retry with a coarser
+        fixed-point step (saturation alone) or for eviction."""
         for slot, bits in zip(slots, host.tolist()):
             a = self.active.get(slot)
-            if bits and a is not None and a[0].failed is None:
-                a[0].failed = int(bits)
-                a[2] = 0  # leaves at the next slice boundary
+            if not bits or a is None or a[0].failed is not None or a[0].retry:
+                continue
+            req = a[0]
+            e = req.fixed_exp or A.FIXED_EXP_DEFAULT
+            if (bits == A.STATUS_SATURATED and req.storage == "i16s" and e > self.min_fixed_exp):
+                req.retry = True
+            else:
+                req.failed = int(bits)
+            a[2] = 0  # leaves at the next slice boundary
 
     def _leave(self, retiring):
         """Members at zero remaining steps leave the batch (no wait); their
@@ -227,8 +260,10 @@ class Server:
         sched = torch.cuda.Stream()
         with cf.ThreadPoolExecutor(self.builders) as pool, torch.cuda.stream(sched):
             n_started = 0
-            while pending or building or self.active or retiring:
+            while pending or building or self.active or retiring or self.requeue:
                 t = now()
+                while self.requeue:  # retries go ahead of new arrivals
+                    pending.appendleft(self.requeue.pop())
                 # admission: arrived requests whose lattice fits the budget go to a builder
                 while pending and pending[0].arrival <= t and \
                         self.used + device_bytes(pending[0].nx, pending[0].ny, pending[0].storage) <= self.budget:
