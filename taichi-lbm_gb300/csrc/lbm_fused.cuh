@@ -242,9 +242,10 @@ struct Storage<LBM_STORE_I16S> {
 // stored step counts in the low half of each word.  The rounding yields
 // t = n + 1.5 * 2^23 as a float, whose bit pattern is that of 1.5 * 2^23
 // plus n, so the step counts add up as integers without a conversion.
-// Returns true when a value left the range (saturated) or was not finite
-// (a NaN fails both range tests).
-__device__ __forceinline__ bool i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9], float iq) {
+// Returns LBM_STATUS_SATURATED when a value left the range (or was NaN),
+// plus LBM_STATUS_NONFINITE when the node's values are NaN (a NaN in a
+// node's moments reaches all nine populations, so population 1 tells).
+__device__ __forceinline__ int i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9], float iq) {
   const unsigned mb = __float_as_uint(I16_MAGIC);
   unsigned s = 0u;  // sum of the steps of populations 1..8 (two's complement)
   bool out = false;
@@ -259,14 +260,15 @@ __device__ __forceinline__ bool i16_conserve_bits(const float (&h)[9], float d, 
   // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is exact
   const int n0 = (int)(__float_as_uint(fmaf(d, iq, I16_MAGIC)) - mb) - (int)s;
   b[0] = (unsigned)min(max(n0, -32768), 32767);
-  return out || n0 < -32768 || n0 > 32767;
+  const bool sat = out || n0 < -32768 || n0 > 32767;
+  return (sat ? LBM_STATUS_SATURATED : 0) | (h[1] != h[1] ? LBM_STATUS_NONFINITE : 0);
 }
 
 // The general (unshifted) path holds f = n Q + w rounded to FP32; the nearest
 // step of f - w recovers n exactly (the FP32 rounding is far below Q / 2).
 // i16_mass: a node's stored sum from its unshifted values (exact), and
 // i16_store_node: the conserving quantisation of a node's post-collision f
-// as int16 step counts (true when a value saturated or was not finite).
+// as int16 step counts (the LBM_STATUS_* bits of i16_conserve_bits).
 __device__ __forceinline__ float i16_mass(const float (&f)[9], const float (&w)[9], float iq, float q) {
   float s = 0.0f;
 #pragma unroll
@@ -281,13 +283,13 @@ __device__ __forceinline__ float i16_mass_rounded(const float (&f)[9], const flo
   for (int k = 0; k < 9; ++k) s += f[k] - w[k];
   return (fmaf(s, iq, I16_MAGIC) - I16_MAGIC) * q;
 }
-__device__ __forceinline__ bool i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
-                                               short (&out)[9], float iq) {
+__device__ __forceinline__ int i16_store_node(const float (&f)[9], const float (&w)[9], float mass,
+                                              short (&out)[9], float iq) {
   float h[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) h[k] = f[k] - w[k];
   unsigned b[9];
-  const bool bad = i16_conserve_bits(h, mass, b, iq);
+  const int bad = i16_conserve_bits(h, mass, b, iq);
 #pragma unroll
   for (int k = 0; k < 9; ++k) out[k] = (short)(b[k] & 0xffffu);
   return bad;
@@ -307,6 +309,15 @@ __device__ __forceinline__ void report_status(int32_t* status, int bit, bool bad
   if (!any || !status) return;
   if ((int)(threadIdx.x & 31) == __ffs(any) - 1) {
     if (!(*(volatile const int32_t*)status & bit)) atomicOr(status, bit);
+  }
+}
+// the same for a set of LBM_STATUS_* bits per lane (OR over the warp)
+__device__ __forceinline__ void report_bits(int32_t* status, int bits) {
+  const unsigned am = __activemask();
+  const int all = __reduce_or_sync(am, (unsigned)bits);
+  if (!all || !status) return;
+  if ((int)(threadIdx.x & 31) == __ffs(am) - 1) {
+    if ((*(volatile const int32_t*)status & all) != all) atomicOr(status, all);
   }
 }
 
@@ -718,19 +729,15 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
-  bool bad = false;  // a colliding node inside the lattice holds NaN or infinity
-#pragma unroll
-  for (int i = 0; i < V; ++i) bad = bad || ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx && not_finite(f[i][0]));
-  report_status(p.status, LBM_STATUS_NONFINITE, bad);
   if constexpr (ST == LBM_STORE_I16S) {
     short q[V][9];
-    bool sat = false;
+    int bits = 0;
 #pragma unroll
     for (int i = 0; i < V; ++i) {
-      const bool b = i16_store_node(f[i], p.wsh, mass[i], q[i], p.fiq);
-      sat = sat || (b && (code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx);
+      const int b = i16_store_node(f[i], p.wsh, mass[i], q[i], p.fiq);
+      if ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx) bits |= b;
     }
-    report_status(p.status, LBM_STATUS_SATURATED, sat);
+    report_bits(p.status, bits);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       T raw[V];
@@ -740,6 +747,10 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
     }
     return;
   }
+  bool bad = false;  // a colliding node inside the lattice holds NaN or infinity
+#pragma unroll
+  for (int i = 0; i < V; ++i) bad = bad || ((code[i] & LBM_CODE_ACTIVE) && x0 + i < p.nx && not_finite(f[i][0]));
+  report_status(p.status, LBM_STATUS_NONFINITE, bad);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     T raw[V];
@@ -793,14 +804,13 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
     const float st = relax_collide<MODEL, PL>(p, f, rho, ux, uy, Fx, Fy, PL ? p.tau[q] : 0.0f);
     if (PL) p.tau[q] = st;
 
-    report_status(p.status, LBM_STATUS_NONFINITE, not_finite(f[0]));
     if constexpr (ST == LBM_STORE_I16S) {
       short n[9];
-      const bool sat = i16_store_node(f, p.wsh, mass, n, p.fiq);
-      report_status(p.status, LBM_STATUS_SATURATED, sat);
+      report_bits(p.status, i16_store_node(f, p.wsh, mass, n, p.fiq));
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = n[k];
     } else {
+      report_status(p.status, LBM_STATUS_NONFINITE, not_finite(f[0]));
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = S::enc(f[k], p.wsh[k], p.fiq);
     }

@@ -479,17 +479,17 @@ __device__ __forceinline__ float node_sum(const float (&h)[9]) {
 // Fixed-point storage: quantise V nodes' post-collision values h with each
 // node's pre-collision mass kept (i16_conserve_bits) and store the nine
 // planes from p (population k at p + k * plane), two step counts per word.
-// Returns true when a value of one of the first nv nodes (the ones inside
-// the lattice; the rest is row padding) saturated or was not finite.
+// Returns the LBM_STATUS_* bits (i16_conserve_bits) of the first nv nodes
+// (the ones inside the lattice; the rest is row padding).
 template <int V>
-__device__ __forceinline__ bool store_i16_conserved(short* p, size_t plane, const float (&h)[V][9],
-                                                    const float (&mass)[V], float iq, int nv) {
+__device__ __forceinline__ int store_i16_conserved(short* p, size_t plane, const float (&h)[V][9],
+                                                   const float (&mass)[V], float iq, int nv) {
   unsigned b[V][9];
-  bool bad = false;
+  int bad = 0;
 #pragma unroll
   for (int i = 0; i < V; ++i) {
-    const bool out = i16_conserve_bits(h[i], mass[i], b[i], iq);
-    bad = bad || (out && i < nv);
+    const int out = i16_conserve_bits(h[i], mass[i], b[i], iq);
+    if (i < nv) bad |= out;
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
@@ -533,15 +533,14 @@ __device__ __forceinline__ void lean_collide_store(const P& p, float (&h)[V][9],
   if (!live) return;
   if (PL) store_vec<float, V>(p.tau + rowoff + x0, tau);
   T* dst = reinterpret_cast<T*>(p.dst);
+  if constexpr (ST == LBM_STORE_I16S) {
+    report_bits(p.status, store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass, p.fiq, p.nx - x0));
+    return;
+  }
   bool bad = false;  // a node inside the lattice holds NaN or infinity
 #pragma unroll
   for (int i = 0; i < V; ++i) bad = bad || (x0 + i < p.nx && not_finite(h[i][0]));
   report_status(p.status, LBM_STATUS_NONFINITE, bad);
-  if constexpr (ST == LBM_STORE_I16S) {
-    const bool sat = store_i16_conserved<V>(dst + rowoff + x0, p.plane, h, mass, p.fiq, p.nx - x0);
-    report_status(p.status, LBM_STATUS_SATURATED, sat);
-    return;
-  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     float c[V];
