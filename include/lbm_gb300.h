@@ -202,6 +202,15 @@ int lbm_sc_update_psi(const LbmLattice* lat, const LbmEos* eos, const int32_t* g
 int lbm_sc_force(const LbmLattice* lat, float g_coh, const int32_t* group, int64_t n, void* stream);
 /* PeriodicPsi_LR (axis 0) / PeriodicPsi_BT (axis 1) — SCBoundaryCondition.py:126-144 */
 int lbm_psi_periodic(const LbmLattice* lat, int32_t axis, void* stream);
+/* OpenNeumannPsi / OpenConvective1orderPsi / OpenConvective2orderPsi /
+ * OpenExtrapolationPsi .apply — SCBoundaryCondition.py:19-110.  group: psi
+ * node coordinates (i, j), halo allowed (-1..NX, -1..NY); the neighbours
+ * x - c_direction and x - 2 c_direction must lie on the psi grid, and for the
+ * convective kinds x - c_direction inside the lattice (its velocity is
+ * averaged over the group). */
+enum { LBM_PSI_OPEN_NEUMANN = 0, LBM_PSI_OPEN_CONV1 = 1, LBM_PSI_OPEN_CONV2 = 2, LBM_PSI_OPEN_EXTRAP = 3 };
+int lbm_psi_open(const LbmLattice* lat, const int32_t* group, int64_t n, int32_t kind, int32_t direction,
+                 void* stream);
 /* FixedPsi.apply — SCBoundaryCondition.py:119-123 */
 int lbm_psi_fixed(const LbmLattice* lat, const int32_t* group, int64_t n, float value, void* stream);
 

@@ -553,6 +553,38 @@ void psi_fixed(Lattice<T>& L, const int32_t* g, int64_t n, double value) {
   for (int64_t m = 0; m < n; ++m) L.psi[L.pid(g[2 * m], g[2 * m + 1])] = T(value);
 }
 
+// SCBoundaryCondition.py:19-110 — open psi boundaries on a group of psi
+// nodes (halo coordinates allowed): kind 0 OpenNeumannPsi, 1
+// OpenConvective1orderPsi, 2 OpenConvective2orderPsi, 3
+// OpenExtrapolationPsi.  The convective kinds first average the velocity of
+// the neighbours x - c_dir over the group, in group order (serially), and
+// take lambda = |U|.
+template <class T>
+void psi_open(Lattice<T>& L, const int32_t* g, int64_t n, int kind, int dir) {
+  const int cx = CX[dir], cy = CY[dir];
+  T lam = T(0);
+  if (kind == 1 || kind == 2) {
+    T Ux = T(0), Uy = T(0);
+    for (int64_t m = 0; m < n; ++m) {
+      size_t q2 = L.id(g[2 * m] - cx, g[2 * m + 1] - cy);
+      Ux = Ux + L.vel[2 * q2];
+      Uy = Uy + L.vel[2 * q2 + 1];
+    }
+    Ux = Ux / T(n);
+    Uy = Uy / T(n);
+    lam = T(1) * std::sqrt(Ux * Ux + Uy * Uy);
+  }
+  for (int64_t m = 0; m < n; ++m) {
+    const int i = g[2 * m], j = g[2 * m + 1];
+    const size_t p = L.pid(i, j), p2 = L.pid(i - cx, j - cy), p3 = L.pid(i - 2 * cx, j - 2 * cy);
+    if (kind == 0) L.psi[p] = L.psi[p2];
+    else if (kind == 1) L.psi[p] = (L.psi[p] + lam * L.psi[p2]) / (T(1) + lam);
+    else if (kind == 2)
+      L.psi[p] = (L.psi[p] + T(2) * lam * L.psi[p2] - T(0.5) * lam * L.psi[p3]) / (T(1) + T(1.5) * lam);
+    else L.psi[p] = T(2) * L.psi[p2] - L.psi[p3];
+  }
+}
+
 // SC force at one node (ExternalForce.py:50-63 and BoundaryCondition.py:301-312)
 template <class T>
 void sc_force_node(Lattice<T>& L, int i, int j, T g_coh) {
@@ -958,6 +990,9 @@ void orc_sc_force(void* p, const int32_t* g, int64_t n, double g_coh) {
 void orc_psi_periodic_lr(void* p) { DISPATCH((Handle*)p, psi_periodic_lr(L)); }
 void orc_psi_periodic_bt(void* p) { DISPATCH((Handle*)p, psi_periodic_bt(L)); }
 void orc_psi_fixed(void* p, const int32_t* g, int64_t n, double v) { DISPATCH((Handle*)p, psi_fixed(L, g, n, v)); }
+void orc_psi_open(void* p, const int32_t* g, int64_t n, int kind, int dir) {
+  DISPATCH((Handle*)p, psi_open(L, g, n, kind, dir));
+}
 
 double orc_get_psi(const double* eos, double rho, double T, int dbl) {
   if (dbl) return get_psi(eos_of(eos), rho, T);

@@ -54,7 +54,7 @@ def lib():
             "orc_mrt_apply": ([vp, vp, i64], None),
             "orc_sc_update_psi": ([vp, vp, i64, vp], None), "orc_sc_force": ([vp, vp, i64, d], None),
             "orc_psi_periodic_lr": ([vp], None), "orc_psi_periodic_bt": ([vp], None),
-            "orc_psi_fixed": ([vp, vp, i64, d], None),
+            "orc_psi_fixed": ([vp, vp, i64, d], None), "orc_psi_open": ([vp, vp, i64, i, i], None),
             "orc_get_psi": ([vp, d, d, i], d),
             "orc_bc_periodic": ([vp, vp, i64], None), "orc_bc_inside": ([vp, vp, i64], None),
             "orc_bc_bounceback": ([vp, vp, i64], None),
@@ -77,6 +77,8 @@ def lib():
 
 
 EOS_KIND = {"sc": 0, "vdw": 1, "rk": 2, "pr": 3, "cs": 4}
+# open psi boundaries (SCBoundaryCondition.py:19-110) -> orc_psi_open kind
+PSI_OPEN = {"open_neumann_psi": 0, "open_conv1_psi": 1, "open_conv2_psi": 2, "open_extrap_psi": 3}
 
 
 def eos_vector(psi):
@@ -263,12 +265,19 @@ def prepare(meta, arrays, nthreads=None):
             else:
                 raise ValueError(f"unknown boundary kind {k}")
 
+    psi_groups = {pb["name"]: np.ascontiguousarray(arrays["g_" + pb["name"]], np.int32).reshape(-1, 2)
+                  for pb in meta.get("psi_bcs", []) if isinstance(pb, dict)}
+
     def apply_psi_bcs():
         for pb in meta.get("psi_bcs", []):
             if pb == "periodic_lr":
                 o.L.orc_psi_periodic_lr(o.h)
             elif pb == "periodic_bt":
                 o.L.orc_psi_periodic_bt(o.h)
+            elif isinstance(pb, dict) and pb["kind"] == "fixed":
+                o.call("psi_fixed", psi_groups[pb["name"]], float(pb["value"]))
+            elif isinstance(pb, dict) and pb["kind"] in PSI_OPEN:
+                o.call("psi_open", psi_groups[pb["name"]], PSI_OPEN[pb["kind"]], int(pb["direction"]))
             else:
                 raise ValueError(pb)
 

@@ -304,6 +304,44 @@ __global__ void k_psi_periodic(LbmLattice L, int axis) {
   }
 }
 
+// SCBoundaryCondition.py:19-110 — open psi boundaries (LBM_PSI_OPEN_*) on
+// a group of psi nodes, one thread walking the group in order: the
+// convective kinds average the velocity of the neighbours x - c_dir over the
+// group first (in group order, as the reference's serial schedule does) and
+// relax towards the neighbours with lambda = |U|.  Each node reads only
+// psi nodes off the group line, so the order of the updates does not matter.
+__global__ void k_psi_open(LbmLattice L, const int32_t* g, int64_t n, int kind, int dir) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  Idx I = idx_of(L);
+  const int cx = cx_dyn(dir), cy = cy_dyn(dir);
+  float lam = 0.0f;
+  if (kind == LBM_PSI_OPEN_CONV1 || kind == LBM_PSI_OPEN_CONV2) {
+    float ux = 0.0f, uy = 0.0f;
+    for (int64_t m = 0; m < n; ++m) {
+      const size_t q2 = I.at(g[2 * m] - cx, g[2 * m + 1] - cy);
+      ux = ux + L.vel[q2];
+      uy = uy + L.vel[I.plane + q2];
+    }
+    ux = ux / (float)n;
+    uy = uy / (float)n;
+    lam = 1.0f * sqrtf(ux * ux + uy * uy);
+  }
+  for (int64_t m = 0; m < n; ++m) {
+    const int i = g[2 * m], j = g[2 * m + 1];
+    float* p = L.psi + psi_at(L, i, j);
+    const float p2 = L.psi[psi_at(L, i - cx, j - cy)];
+    if (kind == LBM_PSI_OPEN_NEUMANN) {
+      *p = p2;
+    } else if (kind == LBM_PSI_OPEN_CONV1) {
+      *p = (*p + lam * p2) / (1.0f + lam);
+    } else {
+      const float p3 = L.psi[psi_at(L, i - 2 * cx, j - 2 * cy)];
+      if (kind == LBM_PSI_OPEN_CONV2) *p = (*p + 2.0f * lam * p2 - 0.5f * lam * p3) / (1.0f + 1.5f * lam);
+      else *p = 2.0f * p2 - p3;
+    }
+  }
+}
+
 // SCBoundaryCondition.py:119-123
 __global__ void k_psi_fixed(LbmLattice L, const int32_t* g, int64_t n, float v) {
   int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -463,10 +501,21 @@ __global__ void k_boundary(LbmLattice L, LbmBoundary b, const int32_t* g, int64_
   }
 }
 
-// One sweep of OpenConvective2order, BoundaryCondition.py:369-390
+// OpenConvective2order, BoundaryCondition.py:369-390: three sweeps over the
+// group, in group order, by one thread.  A node's update reads the psi of
+// the boundary nodes next to it, which the same sweep rewrites, so the
+// result depends on the order the nodes are visited in.  The reference
+// makes its sweep loop the kernel's outermost (parallel) loop and visits the
+// group inside it, which leaves that order to the scheduler; the order
+// here is the serial one, sweep after sweep, node after node.  The group is
+// one boundary line, so one thread is enough.
+__device__ void open_conv2_node(const LbmLattice& L, const LbmBoundary& b, const int32_t* g, int64_t m);
 __global__ void k_open_conv2(LbmLattice L, LbmBoundary b, const int32_t* g, int64_t n) {
-  int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= n) return;
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int it = 0; it < 3; ++it)
+    for (int64_t m = 0; m < n; ++m) open_conv2_node(L, b, g, m);
+}
+__device__ void open_conv2_node(const LbmLattice& L, const LbmBoundary& b, const int32_t* g, int64_t m) {
   Idx I = idx_of(L);
   const size_t P = I.plane;
   const int i = g[2 * m], j = g[2 * m + 1], dir = b.direction;
@@ -719,6 +768,20 @@ int lbm_psi_periodic(const LbmLattice* L, int32_t axis, void* stream) {
   return lbm_err::launch("psi_periodic");
 }
 
+int lbm_psi_open(const LbmLattice* L, const int32_t* g, int64_t n, int32_t kind, int32_t direction,
+                 void* stream) {
+  int rc = check_lat(L, false);
+  if (rc) return rc;
+  if (!L->psi) return lbm_err::set(LBM_ERR_ARG, "psi_open: the lattice has no psi field");
+  if (kind < LBM_PSI_OPEN_NEUMANN || kind > LBM_PSI_OPEN_EXTRAP) return lbm_err::set(LBM_ERR_ARG, "psi_open: kind %d", kind);
+  if (direction < 1 || direction > 4) return lbm_err::set(LBM_ERR_ARG, "psi_open: direction %d", direction);
+  if (n < 0 || (n > 0 && !g)) return lbm_err::set(LBM_ERR_ARG, "psi_open: bad group");
+  if (n && (kind == LBM_PSI_OPEN_CONV1 || kind == LBM_PSI_OPEN_CONV2) && !L->vel)
+    return lbm_err::set(LBM_ERR_ARG, "psi_open: the convective kinds read the velocity field");
+  if (n) k_psi_open<<<1, 32, 0, S_>>>(*L, g, n, kind, direction);
+  return lbm_err::launch("psi_open");
+}
+
 int lbm_psi_fixed(const LbmLattice* L, const int32_t* g, int64_t n, float value, void* stream) {
   CHECK(check_lat(L, false));
   CHECK(check_group(g, n));
@@ -744,7 +807,7 @@ int lbm_boundary_apply(const LbmLattice* L, const LbmBoundary* b, const int32_t*
     case LBM_BC_OPEN_CONV2:
       if (!L->psi || !L->sc_force || !L->temperature)
         return lbm_err::set(LBM_ERR_ARG, "OpenConvective2order needs the Shan-Chen fields");
-      for (int it = 0; it < 3; ++it) k_open_conv2<<<blocks_for(n), TPB, 0, S_>>>(*L, *b, g, n);
+      k_open_conv2<<<1, 32, 0, S_>>>(*L, *b, g, n);
       return lbm_err::launch("open_conv2");
     default:
       if (b->kind < LBM_BC_VELOCITY_BB || b->kind > LBM_BC_OPEN_EXTRAP)

@@ -78,6 +78,8 @@ class LbmPlanDesc(ctypes.Structure):
 FIXED_EXP_DEFAULT, FIXED_EXP_MIN, FIXED_EXP_MAX = 19, 12, 22
 # sticky bits of a plan's device status word
 STATUS_TIMEOUT, STATUS_SATURATED, STATUS_NONFINITE = 1, 2, 4
+# open psi boundary kinds (lbm_psi_open)
+PSI_OPEN_NEUMANN, PSI_OPEN_CONV1, PSI_OPEN_CONV2, PSI_OPEN_EXTRAP = 0, 1, 2, 3
 
 PIPE_DIRECT, PIPE_ASYNC, PIPE_PREFETCH = 0, 1, 2
 ASYNC_TUNINGS = 4
@@ -125,6 +127,8 @@ _SIGS = {
     "lbm_psi_periodic": ([ctypes.POINTER(LbmLattice), ctypes.c_int32, _vp], ctypes.c_int),
     "lbm_psi_fixed": ([ctypes.POINTER(LbmLattice), _vp, ctypes.c_int64, ctypes.c_float, _vp],
                       ctypes.c_int),
+    "lbm_psi_open": ([ctypes.POINTER(LbmLattice), _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _vp],
+                     ctypes.c_int),
     "lbm_boundary_apply": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmBoundary), _vp,
                             ctypes.c_int64, _vp], ctypes.c_int),
     "lbm_plan_create": ([ctypes.POINTER(LbmPlanDesc), ctypes.POINTER(_vp)], ctypes.c_int),

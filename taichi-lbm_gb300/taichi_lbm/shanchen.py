@@ -185,28 +185,50 @@ class FixedPsi(BoundaryCondition):
 
 
 class OpenBoundaryPsi(PlaneBoundary):
-    """SCBoundaryCondition.py:9-15.  The open psi boundaries
-    (OpenNeumannPsi, OpenConvective1orderPsi, OpenConvective2orderPsi,
-    OpenExtrapolationPsi) have no CUDA kernel in this build."""
+    """SCBoundaryCondition.py:9-15: open boundaries of the psi field.  The
+    group is classified over psi coordinates (halo allowed, e.g. with
+    BoundaryClassifier((NX + 2, NY + 2), offset=(-1, -1))); each node is
+    set from its neighbours x - c_direction and x - 2 c_direction."""
+
+    psi_kind = None
+    reads = 1  # psi neighbours read along -c_direction
 
     def apply(self, lb_field):
-        raise NotImplementedError(f"{type(self).__name__} has no CUDA kernel in this build")
+        g = self.group
+        c = lb_field.c[self.direction]
+        g.on(lb_field, halo=1)
+        for d in range(1, self.reads + 1):  # the neighbours lie on the psi grid
+            g.require_inside(lb_field.NX + 2, lb_field.NY + 2, (d * int(c[0]) - 1, d * int(c[1]) - 1),
+                             what=type(self).__name__)
+        if self.psi_kind in (_capi.PSI_OPEN_CONV1, _capi.PSI_OPEN_CONV2):  # and x - c inside the lattice
+            g.require_inside(lb_field.NX, lb_field.NY, (int(c[0]), int(c[1])), what=type(self).__name__)
+        L = lb_field._lattice()
+        _capi.call("lbm_psi_open", ctypes.byref(L), g.ptr, g.n, self.psi_kind, int(self.direction),
+                   stream_handle())
 
 
 class OpenNeumannPsi(OpenBoundaryPsi):
-    pass
+    """SCBoundaryCondition.py:19-34: psi(x) = psi(x - c)."""
+    psi_kind = _capi.PSI_OPEN_NEUMANN
 
 
 class OpenConvective1orderPsi(OpenBoundaryPsi):
-    pass
+    """SCBoundaryCondition.py:36-61: psi(x) = (psi(x) + lambda psi(x - c)) /
+    (1 + lambda), lambda = |u| averaged over the neighbours x - c."""
+    psi_kind = _capi.PSI_OPEN_CONV1
 
 
 class OpenConvective2orderPsi(OpenBoundaryPsi):
-    pass
+    """SCBoundaryCondition.py:64-91: the second-order convective form over
+    x - c and x - 2c."""
+    psi_kind = _capi.PSI_OPEN_CONV2
+    reads = 2
 
 
 class OpenExtrapolationPsi(OpenBoundaryPsi):
-    pass
+    """SCBoundaryCondition.py:94-110: psi(x) = 2 psi(x - c) - psi(x - 2c)."""
+    psi_kind = _capi.PSI_OPEN_EXTRAP
+    reads = 2
 
 
 class BoundaryEngineSC:

@@ -33,6 +33,14 @@ def fixture_names():
                   if f.endswith(".npz") and not f.startswith(("mc_", "ibm_")))
 
 
+def _member_fn_halo(nodes, nx, ny):
+    """Predicate over psi coordinates (-1..NX, -1..NY)."""
+    sel = np.zeros((nx + 2, ny + 2), bool)
+    if nodes.size:
+        sel[nodes[:, 0] + 1, nodes[:, 1] + 1] = True
+    return lambda i, j: sel[np.asarray(i) + 1, np.asarray(j) + 1]
+
+
 def _member_fn(nodes, nx, ny):
     sel = np.zeros((nx, ny), bool)
     if nodes.size:
@@ -84,6 +92,8 @@ def build_from_case(tl, meta, arrays, value_fn_inlet=False):
             bc = tl.OpenConvective1order(spec=spec, direction=d)
         elif k == "open_extrap":
             bc = tl.OpenExtrapolation(spec=spec, direction=d)
+        elif k == "open_conv2":
+            bc = tl.OpenConvective2order(spec=spec, direction=d)
         else:
             raise ValueError(k)
         if inlet_batch and not b["name"].startswith("inlet"):
@@ -112,7 +122,21 @@ def build_from_case(tl, meta, arrays, value_fn_inlet=False):
                                  "psi": model})
         lb.sc_field = sc
         bsc = tl.BoundaryEngineSC()
+        psi_kinds = {"open_neumann_psi": tl.OpenNeumannPsi, "open_conv1_psi": tl.OpenConvective1orderPsi,
+                     "open_conv2_psi": tl.OpenConvective2orderPsi, "open_extrap_psi": tl.OpenExtrapolationPsi}
         for pb in meta.get("psi_bcs", []):
+            if isinstance(pb, dict) and pb["kind"] == "fixed":  # FixedPsi on a recorded group
+                fp = tl.FixedPsi(spec=tl.BoundarySpec(geometry_fn=_member_fn(arrays["g_" + pb["name"]], nx, ny)),
+                                 psi_value=pb["value"])
+                fp.precompute(classifier=cls)
+                bsc.add_boundary_condition(pb["name"], fp)
+                continue
+            if isinstance(pb, dict):  # an open psi boundary on psi coordinates
+                spec = tl.BoundarySpec(geometry_fn=_member_fn_halo(arrays["g_" + pb["name"]], nx, ny))
+                ob = psi_kinds[pb["kind"]](spec, pb["direction"])
+                ob.precompute(classifier=tl.BoundaryClassifier((nx + 2, ny + 2), offset=(-1, -1)))
+                bsc.add_boundary_condition(pb["name"], ob)
+                continue
             bsc.add_boundary_condition(pb, tl.PeriodicPsi_LR() if pb == "periodic_lr" else tl.PeriodicPsi_BT())
         lb.T.from_numpy(np.asarray(arrays["T"], np.float32) if "T" in arrays
                         else np.full((nx, ny), meta.get("T", 1.0), np.float32))

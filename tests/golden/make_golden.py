@@ -258,9 +258,15 @@ def make_collision(ti, tl, case, lb, group, collision, nu, fluid_model, tau_clam
 
 
 def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bgk", {}),
-                   nu=0.5 / 3.0, T=1.0, gravity=None):
+                   nu=0.5 / 3.0, T=1.0, gravity=None, fixed_psi=None, open_conv2=False, open_psi=None):
     """Fully periodic single-component Shan-Chen lattice (the two-phase
-    separation pattern of ``Bubble or two-phase separation.py``)."""
+    separation pattern of ``Bubble or two-phase separation.py``).
+    fixed_psi=(row, value): a FixedPsi on the nodes of that row, applied
+    after the periodic psi boundaries.  open_conv2: an OpenConvective2order
+    outlet (direction 1) on the last column, applied after the stream.
+    open_psi=[(kind, row, direction), ...]: open psi boundaries on the psi
+    nodes (i, row), 0 <= i < NX (halo rows allowed), classified over the
+    psi grid; psi is then periodic in x only, and these follow."""
     lb = tl.LBField(case.meta["name"], nx, ny, 1)
     if gravity is not None:
         lb.set_gravity(ti.Vector(list(gravity)))
@@ -279,6 +285,14 @@ def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bg
     per.precompute(classifier=cls)
     be.add_boundary_condition("stream", per)
     case.bc("stream", "periodic", group_nodes(per.group))
+    if open_conv2:
+        @ti.func
+        def outlet_fn(i, j):
+            return lb.mask[i, j] == 1 and i == nx - 1
+        oc = tl.OpenConvective2order(spec=tl.BoundarySpec(geometry_fn=outlet_fn), direction=1)
+        oc.precompute(classifier=cls)
+        be.add_boundary_condition("outlet", oc)
+        case.bc("outlet", "open_conv2", group_nodes(oc.group), direction=1)
     lb.neighbor_classify()
     me = tl.MacroscopicEngine(fluid.group)
     coll = make_collision(ti, tl, case, lb, fluid.group, collision, nu, None, None, None)
@@ -296,8 +310,38 @@ def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bg
                                       "psi": psi})
     bsc = tl.BoundaryEngineSC()
     bsc.add_boundary_condition("periodicLR", tl.PeriodicPsi_LR())
-    bsc.add_boundary_condition("periodicBT", tl.PeriodicPsi_BT())
-    case.meta["psi_bcs"] = ["periodic_lr", "periodic_bt"]
+    case.meta["psi_bcs"] = ["periodic_lr"]
+    if open_psi:
+        cls_psi = tl.BoundaryClassifier(ti.field(float, shape=(nx + 2, ny + 2), offset=(-1, -1)))
+        kinds = {"open_neumann_psi": tl.OpenNeumannPsi, "open_conv1_psi": tl.OpenConvective1orderPsi,
+                 "open_conv2_psi": tl.OpenConvective2orderPsi, "open_extrap_psi": tl.OpenExtrapolationPsi}
+        for n_, (kind, row, direction) in enumerate(open_psi):
+            def make(r):
+                @ti.func
+                def fn(i, j):
+                    return j == r and i >= 0 and i < nx
+                return fn
+            ob = kinds[kind](tl.BoundarySpec(geometry_fn=make(row)), direction)
+            ob.precompute(classifier=cls_psi)
+            name = f"psi_{kind}_{n_}"
+            bsc.add_boundary_condition(name, ob)
+            case.meta["psi_bcs"].append({"kind": kind, "name": name, "direction": int(direction)})
+            case.groups["g_" + name] = np.asarray(sorted(map(tuple, group_nodes(ob.group))),
+                                                  np.int32).reshape(-1, 2)
+    else:
+        bsc.add_boundary_condition("periodicBT", tl.PeriodicPsi_BT())
+        case.meta["psi_bcs"].append("periodic_bt")
+    if fixed_psi is not None:
+        row, value = fixed_psi
+
+        @ti.func
+        def row_fn(i, j):
+            return lb.mask[i, j] == 1 and j == row
+        fp = tl.FixedPsi(spec=tl.BoundarySpec(geometry_fn=row_fn), psi_value=value)
+        fp.precompute(classifier=cls)
+        bsc.add_boundary_condition("fixed", fp)
+        case.meta["psi_bcs"].append({"kind": "fixed", "name": "psi_fixed", "value": float(value)})
+        case.groups["g_psi_fixed"] = np.asarray(sorted(map(tuple, group_nodes(fp.group))), np.int32).reshape(-1, 2)
 
     lb.T.fill(T)
     case.meta["T"] = T
@@ -541,6 +585,51 @@ def case_table():
                                             g_coh=-1.0, rho_init=rho_vdw,
                                             collision=("trt", {"magic": [0.25]}), nu=0.1,
                                             T=0.85 * 4.0 / 7.0), "shanchen", 30, "f64", (16, 16))
+    # Redlich-Kwong and Peng-Robinson pseudopotentials (EOS.py:61-83), the
+    # Yuan-Schaefer parameters a = 2/49, b = 2/21, R = 1, near their critical
+    # densities at T = 0.9 Tc.  These cases draw from their own generator, so
+    # the inputs of the cases after them stay as they were.
+    rng2 = np.random.Generator(np.random.PCG64(SEED + 1))
+    rk = {"a": 2.0 / 49.0, "b": 2.0 / 21.0, "R": 1.0, "G": -1.0, "rho_cr": 2.729,
+          "pressure_cr": 0.1779, "temperature_cr": 0.1961}
+    rho_rk = (2.6 * (1.0 + rng2.uniform(-0.01, 0.01, size=(24, 20)))).astype(np.float64)
+    t["sc_rk_bgk_f32"] = ("shanchen", dict(eos=("rk", rk), g_coh=-1.0, rho_init=rho_rk,
+                                           collision=("bgk", {}), nu=0.5 / 3.0, T=0.9 * 0.1961),
+                          "shanchen", 30, "f32", (24, 20))
+    pr = {"a": 2.0 / 49.0, "b": 2.0 / 21.0, "R": 1.0, "G": -1.0, "rho_cr": 2.657,
+          "pressure_cr": 0.0585, "temperature_cr": 0.0729, "omega": 0.344}
+    rho_pr = (2.5 * (1.0 + rng2.uniform(-0.01, 0.01, size=(20, 16)))).astype(np.float64)
+    t["sc_pr_trt_f32"] = ("shanchen", dict(eos=("pr", pr), g_coh=-1.0, rho_init=rho_pr,
+                                           collision=("trt", {"magic": [0.25]}), nu=0.1, T=0.9 * 0.0729),
+                          "shanchen", 30, "f32", (20, 16))
+    # FixedPsi (SCBoundaryCondition.py:113-123) on the bottom row, after the
+    # periodic psi boundaries
+    rho_fx = (np.log(2.0) + 0.1 * rng2.uniform(0.0, 1.0, size=(20, 18))).astype(np.float64)
+    t["sc_fixedpsi_bgk_f32"] = ("shanchen", dict(eos=("sc", 1.0), g_coh=-5.0, rho_init=rho_fx,
+                                                 collision=("bgk", {}), nu=0.1, T=1.0, fixed_psi=(0, 0.3)),
+                                "shanchen", 30, "f32", (20, 18))
+    # OpenConvective2order (BoundaryCondition.py:362-390) on the last column
+    # of a Shan-Chen lattice, after the periodic stream
+    rho_oc = (0.25 * (1.0 + rng2.uniform(-0.01, 0.01, size=(24, 20)))).astype(np.float64)
+    p_oc, T_oc = cs_params(0.85)
+    t["sc_openconv2_bgk_f32"] = ("shanchen", dict(eos=("cs", p_oc), g_coh=-1.0, rho_init=rho_oc,
+                                                  collision=("bgk", {}), nu=0.5 / 3.0, T=T_oc, open_conv2=True),
+                                 "shanchen", 30, "f32", (24, 20))
+    # the open psi boundaries (SCBoundaryCondition.py:19-110) on the halo rows
+    # below and above the lattice (psi periodic in x)
+    rho_op = (0.25 * (1.0 + rng2.uniform(-0.01, 0.01, size=(24, 20)))).astype(np.float64)
+    p_op, T_op = cs_params(0.8)
+    t["sc_openpsi_bgk_f32"] = ("shanchen", dict(eos=("cs", p_op), g_coh=-1.0, rho_init=rho_op,
+                                                collision=("bgk", {}), nu=0.5 / 3.0, T=T_op,
+                                                open_psi=[("open_neumann_psi", 20, 2),
+                                                          ("open_extrap_psi", -1, 4)]),
+                               "shanchen", 30, "f32", (24, 20))
+    t["sc_openpsiconv_trt_f32"] = ("shanchen", dict(eos=("cs", p_op), g_coh=-1.0, rho_init=rho_op,
+                                                    collision=("trt", {"magic": [0.25]}), nu=0.1, T=T_op,
+                                                    gravity=(1e-5, 0.0),
+                                                    open_psi=[("open_conv1_psi", 20, 2),
+                                                              ("open_conv2_psi", -1, 4)]),
+                                   "shanchen", 30, "f32", (24, 20))
     # two components: a disc of component 0 in component 1, seeded noise
     mx, my = 24, 20
     ii, jj = np.meshgrid(np.arange(mx), np.arange(my), indexing="ij")
