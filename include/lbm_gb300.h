@@ -219,6 +219,65 @@ int lbm_psi_fixed(const LbmLattice* lat, const int32_t* group, int64_t n, float 
 int lbm_boundary_apply(const LbmLattice* lat, const LbmBoundary* bc, const int32_t* group,
                        int64_t n, void* stream);
 
+/* ----------------------------------------------------------- multi-component
+ * LBField with num_components > 1 (taichi_lbm/lbm.py:5-56) and the
+ * two-component Shan-Chen model (ExternalForce.py:66-117).  Arrays are
+ * component-major: component c's block follows component c-1's.  The
+ * mixture fields (total_rho, total_pressure, vel, temperature) are single. */
+#define LBM_MC_MAX 4
+typedef struct LbmMCLattice {
+  int32_t nx, ny, pitch, psi_pitch;
+  int32_t nc;             /* components, 1..LBM_MC_MAX                       */
+  float* f;               /* [nc][9][ny][pitch] post-stream populations      */
+  float* f2;              /* [nc][9][ny][pitch] post-collision populations   */
+  float* rho;             /* [nc][ny][pitch]                                 */
+  float* total_rho;       /* [ny][pitch]                                     */
+  float* pressure;        /* [nc][ny][pitch]                                 */
+  float* total_pressure;  /* [ny][pitch]                                     */
+  float* temperature;     /* [ny][pitch]                                     */
+  float* vel;             /* [2][ny][pitch] mixture velocity                 */
+  float* body_force;      /* [nc][2][ny][pitch]                              */
+  float* sc_force;        /* [nc][2][ny][pitch]                              */
+  float* psi;             /* [nc][ny+2][psi_pitch] one-node halo             */
+  float gravity[2];
+} LbmMCLattice;
+/* ShanChenForceC2's parameters (ExternalForce.py:67-84): cohesion matrix
+ * g_coh, adhesion g_adh per component, the two pseudopotentials (psi_list),
+ * and fluid_strategy evaluated on the psi grid: fluid[(j+1)*psi_pitch + i+1]
+ * = 1 where fluid_strategy(i, j) holds, for i in -1..NX, j in -1..NY.       */
+typedef struct LbmMCShanChen {
+  float g_coh[LBM_MC_MAX][LBM_MC_MAX];
+  float g_adh[LBM_MC_MAX];
+  LbmEos eos[LBM_MC_MAX];
+  const uint8_t* fluid;
+} LbmMCShanChen;
+/* LBField.init_LBM — lbm.py:119-125, every component */
+int lbm_mc_init_feq(const LbmMCLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.density — lbm.py:153-164 */
+int lbm_mc_density(const LbmMCLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.pressure2 — lbm.py:185-202 */
+int lbm_mc_pressure2(const LbmMCLattice* lat, const LbmMCShanChen* sc, const int32_t* group, int64_t n,
+                     void* stream);
+/* ShanChenForceC2.update_psi — ExternalForce.py:86-92 */
+int lbm_mc_update_psi(const LbmMCLattice* lat, const LbmMCShanChen* sc, const int32_t* group, int64_t n,
+                      void* stream);
+/* PeriodicPsi_LR (axis 0) / PeriodicPsi_BT (axis 1), every component —
+ * SCBoundaryCondition.py:126-144 */
+int lbm_mc_psi_periodic(const LbmMCLattice* lat, int32_t axis, void* stream);
+/* ShanChenForceC2.cau_SCforce — ExternalForce.py:96-117 */
+int lbm_mc_sc_force(const LbmMCLattice* lat, const LbmMCShanChen* sc, const int32_t* group, int64_t n,
+                    void* stream);
+/* MacroscopicEngine.force_density — lbm.py:215-220 */
+int lbm_mc_force_density(const LbmMCLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* MacroscopicEngine.velocity (mixture) — lbm.py:223-237 */
+int lbm_mc_velocity(const LbmMCLattice* lat, const int32_t* group, int64_t n, void* stream);
+/* BGKCollision.apply, every component — CollisionEngine.py:96-110;
+ * tau: [nc][ny][pitch] relaxation times (BGKCollision.tau) */
+int lbm_mc_bgk_apply(const LbmMCLattice* lat, const float* tau, const int32_t* group, int64_t n,
+                     void* stream);
+/* PeriodicAllBoundary.apply, every component — BoundaryCondition.py:419-432 */
+int lbm_mc_stream_periodic(const LbmMCLattice* lat, const int32_t* group, int64_t n, void* stream);
+
 /* ----------------------------------------------------------- fused plan
  * The whole step composed the way the reference's example drivers compose it
  * (cases/Circular cylinder.py:182-193; cases/Power Law Fluid.py:160-173):

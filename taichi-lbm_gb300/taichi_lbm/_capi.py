@@ -52,6 +52,21 @@ class LbmEos(ctypes.Structure):
                 ("omega", ctypes.c_float), ("T_cr", ctypes.c_float)]
 
 
+MC_MAX = 4
+
+
+class LbmMCLattice(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("pitch", ctypes.c_int32),
+                ("psi_pitch", ctypes.c_int32), ("nc", ctypes.c_int32)] + [
+        (n, _vp) for n in ("f", "f2", "rho", "total_rho", "pressure", "total_pressure", "temperature",
+                           "vel", "body_force", "sc_force", "psi")] + [("gravity", ctypes.c_float * 2)]
+
+
+class LbmMCShanChen(ctypes.Structure):
+    _fields_ = [("g_coh", (ctypes.c_float * MC_MAX) * MC_MAX), ("g_adh", ctypes.c_float * MC_MAX),
+                ("eos", LbmEos * MC_MAX), ("fluid", _vp)]
+
+
 class LbmBoundary(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("direction", ctypes.c_int32),
                 ("rho_value", ctypes.c_float), ("velocity", ctypes.c_float * 2),
@@ -129,6 +144,16 @@ _SIGS = {
                       ctypes.c_int),
     "lbm_psi_open": ([ctypes.POINTER(LbmLattice), _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _vp],
                      ctypes.c_int),
+    "lbm_mc_init_feq": ([ctypes.POINTER(LbmMCLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_density": ([ctypes.POINTER(LbmMCLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_pressure2": ([ctypes.POINTER(LbmMCLattice), ctypes.POINTER(LbmMCShanChen), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_update_psi": ([ctypes.POINTER(LbmMCLattice), ctypes.POINTER(LbmMCShanChen), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_psi_periodic": ([ctypes.POINTER(LbmMCLattice), ctypes.c_int32, _vp], ctypes.c_int),
+    "lbm_mc_sc_force": ([ctypes.POINTER(LbmMCLattice), ctypes.POINTER(LbmMCShanChen), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_force_density": ([ctypes.POINTER(LbmMCLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_velocity": ([ctypes.POINTER(LbmMCLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_bgk_apply": ([ctypes.POINTER(LbmMCLattice), _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "lbm_mc_stream_periodic": ([ctypes.POINTER(LbmMCLattice), _vp, ctypes.c_int64, _vp], ctypes.c_int),
     "lbm_boundary_apply": ([ctypes.POINTER(LbmLattice), ctypes.POINTER(LbmBoundary), _vp,
                             ctypes.c_int64, _vp], ctypes.c_int),
     "lbm_plan_create": ([ctypes.POINTER(LbmPlanDesc), ctypes.POINTER(_vp)], ctypes.c_int),

@@ -236,6 +236,15 @@ class BoundaryCondition:
     def apply(self, lb_field):
         if self.kind == _capi.BC_FLUID:
             return
+        if lb_field.nc > 1:
+            if self.kind != _capi.BC_PERIODIC:
+                raise NotImplementedError(f"{type(self).__name__} on a multi-component lattice: only "
+                                          "PeriodicAllBoundary streams every component in this build")
+            self.group.require_inside(lb_field.NX, lb_field.NY, what=type(self).__name__)
+            L = lb_field._mclattice()
+            _capi.call("lbm_mc_stream_periodic", ctypes.byref(L), self.group.ptr, self.group.n,
+                       stream_handle())
+            return
         self.check(lb_field)
         lb_field._sync_fused()
         L = lb_field._lattice()

@@ -86,11 +86,12 @@ class Collision:
     def _setup(self, params):
         p = dict(params)
         self.NX, self.NY = int(p["NX"]), int(p["NY"])
-        if int(p.get("num_components") or 1) != 1:
-            raise NotImplementedError("single-component collisions only in this build")
+        self.nc = int(p.get("num_components") or 1)
+        if self.nc != 1 and self.model != _capi.BGK:
+            raise NotImplementedError("multi-component lattices collide with BGKCollision in this build")
         self.pitch = round_up(self.NX, 32)
         self.device = self.group.group.device
-        self.nu = np.asarray(p["shearviscosity"], np.float32).reshape(-1)[:1]
+        self.nu = np.asarray(p["shearviscosity"], np.float32).reshape(-1)[:max(1, self.nc)]
         clamp = p.get("tau_clamp")
         if clamp is not None:
             self.tau_min, self.tau_max = float(clamp[0]), float(clamp[1])
@@ -127,6 +128,14 @@ class Collision:
         return c
 
     def _call(self, fn, lb_field, init=False):
+        if lb_field.nc > 1:
+            if fn != "lbm_collision_apply":
+                raise NotImplementedError("multi-component lattices: BGK collision with Newtonian "
+                                          "components only (no local relaxation)")
+            L = lb_field._mclattice()
+            _capi.call("lbm_mc_bgk_apply", ctypes.byref(L), ctypes.c_void_p(self._tau.data_ptr()),
+                       self.group.on(lb_field).ptr, self.group.n, stream_handle())
+            return
         lb_field._sync_fused()
         L = lb_field._lattice()
         c = self._init_struct() if init else self._struct()
@@ -161,6 +170,16 @@ class BGKCollision(Collision):
         p.update(params)
         super().__init__(p["group"], p["fluid_model"])
         self._setup(p)
+        if self.nc > 1:
+            # one relaxation time per component: tau = 3 nu_c + 1/2 on the
+            # group (CollisionEngine.py:65-70), in float32 as the reference
+            self._tau = alloc((self.nc, self.NY, self.pitch), self.device)
+            self.tau = Field(self, "_tau", self.NX, self.NY, "sc", nc=self.nc)
+            nd = torch.as_tensor(self.group.nodes, device=self.device).long()
+            for c in range(self.nc):
+                t = torch.tensor(float(self.nu[c]), dtype=torch.float32) * 3.0 + 0.5
+                self._tau[c][nd[:, 1], nd[:, 0]] = t.to(self.device)
+            return
         self._tau = alloc((self.NY, self.pitch), self.device)
         self.tau = Field(self, "_tau", self.NX, self.NY, "sc")
         self.initTau()

@@ -39,12 +39,16 @@ class Field:
       ``"v"``   n-vector per node, shape (NX, NY, n)
       ``"vc"``  n-vector per node and component, shape (NX, NY, 1, n)
     The tensor is ``[ny][pitch]`` (scalars) or ``[n][ny][pitch]`` (vectors);
-    ``halo`` = 1 means one extra node on every side (index -1 .. NX).
+    ``halo`` = 1 means one extra node on every side (index -1 .. NX).  With
+    nc > 1 components the per-component kinds ("sc", "vc") hold a leading
+    component axis: ``[nc][ny][pitch]`` / ``[nc][n][ny][pitch]``, shape
+    (NX, NY, nc) / (NX, NY, nc, n) in reference order.
     """
 
-    def __init__(self, owner, attr, nx, ny, kind, n=None, halo=0):
+    def __init__(self, owner, attr, nx, ny, kind, n=None, halo=0, nc=1):
         self._owner, self._attr = owner, attr
         self.nx, self.ny, self.kind, self.n, self.halo = nx, ny, kind, n, halo
+        self.nc = int(nc) if kind in ("sc", "vc") else 1
 
     @property
     def tensor(self):
@@ -53,13 +57,17 @@ class Field:
     @property
     def shape(self):
         nx, ny = self.nx + 2 * self.halo, self.ny + 2 * self.halo
-        return {"s": (nx, ny), "sc": (nx, ny, 1), "v": (nx, ny, self.n),
-                "vc": (nx, ny, 1, self.n)}[self.kind]
+        return {"s": (nx, ny), "sc": (nx, ny, self.nc), "v": (nx, ny, self.n),
+                "vc": (nx, ny, self.nc, self.n)}[self.kind]
 
     def _view(self):
         """Tensor view in reference order (device)."""
         t = self.tensor
         w = self.nx + 2 * self.halo
+        if self.nc > 1:
+            if self.kind == "sc":  # [nc][ny][pitch] -> (nx, ny, nc)
+                return t[:, :, :w].permute(2, 1, 0)
+            return t[:, :, :, :w].permute(3, 2, 0, 1)  # [nc][n][ny][pitch] -> (nx, ny, nc, n)
         if self.kind in ("s", "sc"):
             v = t[:, :w].transpose(0, 1)
             return v.unsqueeze(-1) if self.kind == "sc" else v
@@ -86,11 +94,16 @@ class Field:
         else:
             vals = np.broadcast_to(np.asarray(v, dtype=np.float32), (self.n,))
             for c in range(self.n):
-                self.tensor[c].fill_(float(vals[c]))
+                if self.nc > 1:
+                    self.tensor[:, c].fill_(float(vals[c]))
+                else:
+                    self.tensor[c].fill_(float(vals[c]))
 
     def _key(self, key):
         if not isinstance(key, tuple):
             key = (key,)
+        if self.nc > 1:
+            return None  # indexed through the reference-order copy
         if all(isinstance(k, (int, np.integer)) for k in key):
             i, j = int(key[0]) + self.halo, int(key[1]) + self.halo
             rest = key[2:]

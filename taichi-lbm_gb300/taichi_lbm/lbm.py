@@ -64,45 +64,50 @@ class NeighborView:
 class LBField:
     """Lattice state of one D2Q9 simulation (taichi_lbm/lbm.py:5-142).
 
-    Single component: the multi-component paths of the reference
-    (pressure2, ShanChenForceC2) are not part of this build.
+    num_components > 1 (up to 4) keeps one set of populations, density,
+    pressure, psi, Shan-Chen force and body force per component (the
+    component-major LbmMCLattice layout) beside the mixture fields; such a
+    lattice runs the per-stage multi-component kernels (MacroscopicEngine,
+    ShanChenForceC2, BGKCollision, PeriodicAllBoundary, PeriodicPsi_LR/BT).
     """
 
     def __init__(self, name, NX, NY, num_components, device=None):
-        if int(num_components) != 1:
-            raise NotImplementedError("this build runs single-component lattices "
-                                      "(num_components=1); multi-component Shan-Chen is not built")
+        nc = int(num_components)
+        if not 1 <= nc <= _capi.MC_MAX:
+            raise ValueError(f"num_components must be 1..{_capi.MC_MAX}")
         dev = cuda_device(device)
         self.device = dev
         self.name = name
         self.NX, self.NY = int(NX), int(NY)
-        self.num_components = Scalar0D(1)
+        self.nc = nc
+        self.num_components = Scalar0D(nc)
         self.pitch = round_up(self.NX, 32)
         self.psi_pitch = round_up(self.NX + 2, 32)
         nx, ny, P = self.NX, self.NY, self.pitch
-        self._f = alloc((9, ny, P), dev)
-        self._f2 = alloc((9, ny, P), dev)
-        self._rho = alloc((ny, P), dev)
+        lead = (nc,) if nc > 1 else ()  # per-component arrays: a leading component axis
+        self._f = alloc(lead + (9, ny, P), dev)
+        self._f2 = alloc(lead + (9, ny, P), dev)
+        self._rho = alloc(lead + (ny, P), dev)
         self._total_rho = alloc((ny, P), dev)
-        self._pressure = alloc((ny, P), dev)
+        self._pressure = alloc(lead + (ny, P), dev)
         self._total_pressure = alloc((ny, P), dev)
-        self._shear_rate = alloc((ny, P), dev)
+        self._shear_rate = alloc(lead + (ny, P), dev)
         self._T = alloc((ny, P), dev)
         self._vel = alloc((2, ny, P), dev)
-        self._body_force = alloc((2, ny, P), dev)
-        self._SCforce = alloc((2, ny, P), dev)
-        self._psi = alloc((ny + 2, self.psi_pitch), dev)
+        self._body_force = alloc(lead + (2, ny, P), dev)
+        self._SCforce = alloc(lead + (2, ny, P), dev)
+        self._psi = alloc(lead + (ny + 2, self.psi_pitch), dev)
         self._mask_dev = alloc((ny, P), dev, torch.int32)
         self._links = alloc((ny, P), dev, torch.int16)
         self._mask_version = -1
 
-        self.f = Field(self, "_f", nx, ny, "vc", 9)
-        self.f2 = Field(self, "_f2", nx, ny, "vc", 9)
-        self.rho = Field(self, "_rho", nx, ny, "sc")
-        self.pressure = Field(self, "_pressure", nx, ny, "sc")
-        self.body_force = Field(self, "_body_force", nx, ny, "vc", 2)
-        self.shear_rate = Field(self, "_shear_rate", nx, ny, "sc")
-        self.SCforce = Field(self, "_SCforce", nx, ny, "vc", 2)
+        self.f = Field(self, "_f", nx, ny, "vc", 9, nc=nc)
+        self.f2 = Field(self, "_f2", nx, ny, "vc", 9, nc=nc)
+        self.rho = Field(self, "_rho", nx, ny, "sc", nc=nc)
+        self.pressure = Field(self, "_pressure", nx, ny, "sc", nc=nc)
+        self.body_force = Field(self, "_body_force", nx, ny, "vc", 2, nc=nc)
+        self.shear_rate = Field(self, "_shear_rate", nx, ny, "sc", nc=nc)
+        self.SCforce = Field(self, "_SCforce", nx, ny, "vc", 2, nc=nc)
         self.vel = Field(self, "_vel", nx, ny, "v", 2)
         self.total_rho = Field(self, "_total_rho", nx, ny, "s")
         self.total_pressure = Field(self, "_total_pressure", nx, ny, "s")
@@ -132,8 +137,19 @@ class LBField:
             self._mask_dev[:, :self.NX].copy_(m)
             self._mask_version = self.mask.version
 
-    def _lattice(self):
-        """The LbmLattice struct for the current buffers."""
+    def _lattice(self, geometry_only=False):
+        """The LbmLattice struct for the current buffers (geometry_only: just
+        the mask and link table, for any number of components)."""
+        if self.nc > 1 and geometry_only:
+            self._sync_mask()
+            L = _capi.LbmLattice()
+            L.nx, L.ny, L.pitch, L.psi_pitch = self.NX, self.NY, self.pitch, self.psi_pitch
+            L.mask = self._mask_dev.data_ptr()
+            L.links = self._links.data_ptr()
+            return L
+        if self.nc > 1:
+            raise NotImplementedError("this operation runs on single-component lattices; a "
+                                      f"{self.nc}-component lattice runs the multi-component kernels")
         self._sync_mask()
         L = _capi.LbmLattice()
         L.nx, L.ny, L.pitch, L.psi_pitch = self.NX, self.NY, self.pitch, self.psi_pitch
@@ -144,6 +160,18 @@ class LBField:
         L.sc_force = self._SCforce.data_ptr()
         L.mask = self._mask_dev.data_ptr()
         L.links = self._links.data_ptr()
+        g = np.asarray(self.gravity_force, np.float32).reshape(2)
+        L.gravity[0], L.gravity[1] = float(g[0]), float(g[1])
+        return L
+
+    def _mclattice(self):
+        """The LbmMCLattice struct (every component) for the current buffers."""
+        L = _capi.LbmMCLattice()
+        L.nx, L.ny, L.pitch, L.psi_pitch, L.nc = self.NX, self.NY, self.pitch, self.psi_pitch, self.nc
+        for name in ("f", "f2", "rho", "total_rho", "pressure", "total_pressure", "vel", "body_force", "psi"):
+            setattr(L, name, getattr(self, "_" + name).data_ptr())
+        L.temperature = self._T.data_ptr()
+        L.sc_force = self._SCforce.data_ptr()
         g = np.asarray(self.gravity_force, np.float32).reshape(2)
         L.gravity[0], L.gravity[1] = float(g[0]), float(g[1])
         return L
@@ -183,12 +211,16 @@ class LBField:
         if self.keep_init_snapshot:  # host copy of the initial moments, for case descriptions
             self._init_snapshot = (self.rho.to_numpy()[:, :, 0].copy(), self.vel.to_numpy().copy(),
                                    self.T.to_numpy().copy())
+        if self.nc > 1:
+            L = self._mclattice()
+            _capi.call("lbm_mc_init_feq", ctypes.byref(L), group.on(self).ptr, group.n, stream_handle())
+            return
         L = self._lattice()
         _capi.call("lbm_init_feq", ctypes.byref(L), group.on(self).ptr, group.n, stream_handle())
 
     def neighbor_classify(self):
         """Pull-source table from the mask (lbm.py:127-142)."""
-        L = self._lattice()
+        L = self._lattice(geometry_only=True)
         _capi.call("lbm_neighbor_classify", ctypes.byref(L), stream_handle())
 
     def links_host(self):
@@ -204,12 +236,23 @@ class MacroscopicEngine:
     def time_updata(self, lb_field):
         lb_field.time[None] = lb_field.time[None] + 1
 
+    def _mc(self, fn, lb_field, *extra):
+        L = lb_field._mclattice()
+        _capi.call(fn, ctypes.byref(L), *extra, self.group.on(lb_field).ptr, self.group.n, stream_handle())
+
     def density(self, lb_field):
+        if lb_field.nc > 1:
+            return self._mc("lbm_mc_density", lb_field)
         lb_field._sync_fused()
         L = lb_field._lattice()
         _capi.call("lbm_density", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n, stream_handle())
 
     def pressure(self, lb_field):
+        if lb_field.nc > 1:  # pressure2 (lbm.py:185-202)
+            sc = lb_field.sc_field
+            if sc is None or not hasattr(sc, "mc_struct"):
+                raise NotImplementedError("a multi-component lattice's pressure needs ShanChenForceC2")
+            return self._mc("lbm_mc_pressure2", lb_field, ctypes.byref(sc.mc_struct()))
         lb_field._sync_fused()
         L = lb_field._lattice()
         sc = lb_field.sc_field
@@ -218,14 +261,19 @@ class MacroscopicEngine:
 
     pressure0 = pressure
     pressure1 = pressure
+    pressure2 = pressure
 
     def force_density(self, lb_field):
+        if lb_field.nc > 1:
+            return self._mc("lbm_mc_force_density", lb_field)
         lb_field._sync_fused()
         L = lb_field._lattice()
         _capi.call("lbm_force_density", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n,
                    stream_handle())
 
     def velocity(self, lb_field):
+        if lb_field.nc > 1:
+            return self._mc("lbm_mc_velocity", lb_field)
         lb_field._sync_fused()
         L = lb_field._lattice()
         _capi.call("lbm_velocity", ctypes.byref(L), self.group.on(lb_field).ptr, self.group.n, stream_handle())

@@ -1,12 +1,13 @@
 """Shan-Chen pseudopotential model: equations of state (taichi_lbm/EOS.py),
-the single-component force (taichi_lbm/ExternalForce.py) and psi boundaries
-(taichi_lbm/SCBoundaryCondition.py)."""
+the single- and two-component forces (taichi_lbm/ExternalForce.py) and psi
+boundaries (taichi_lbm/SCBoundaryCondition.py)."""
 import ctypes
 
 import numpy as np
+import torch
 
 from . import _capi
-from .boundary import BoundaryCondition, PlaneBoundary
+from .boundary import BoundaryCondition, PlaneBoundary, evaluate_predicate
 from .fields import Field
 from .lbm import WEIGHTS, C, stream_handle
 
@@ -119,7 +120,7 @@ class ShanChenModel:
     def __init__(self, lb_field, group):
         self.group = group
         self.wc = (WEIGHTS[:, None] * C).astype(np.float32)
-        self.psi_field = Field(lb_field, "_psi", lb_field.NX, lb_field.NY, "sc", halo=1)
+        self.psi_field = Field(lb_field, "_psi", lb_field.NX, lb_field.NY, "sc", halo=1, nc=lb_field.nc)
 
 
 class ShanChenForceC1(ShanChenModel):
@@ -147,28 +148,80 @@ class ShanChenForceC1(ShanChenModel):
 
 
 class ShanChenForceC2(ShanChenModel):
-    """ExternalForce.py:66-117 (two components) — not part of this build."""
+    """ExternalForce.py:66-117: two-component Shan-Chen force on a lattice
+    with num_components = 2.  params: lb_field, g_coh (cohesion matrix,
+    nc x nc), gadh (adhesion per component), group, psi_list (the two
+    components' pseudopotentials) and fluid_strategy(x, y), a predicate that
+    may be called on halo coordinates (-1..NX, -1..NY): cohesion acts from
+    neighbours where it holds, adhesion from the others."""
 
     def __init__(self, params):
-        raise NotImplementedError("two-component Shan-Chen (ShanChenForceC2) is not built; "
-                                  "this build runs single-component lattices")
+        p = {"lb_field": None, "g_coh": None, "gadh": None, "group": None, "psi_list": None,
+             "fluid_strategy": None}
+        p.update(params)
+        lb = p["lb_field"]
+        if lb.nc < 2:
+            raise ValueError("ShanChenForceC2 needs a lattice with num_components >= 2")
+        super().__init__(lb, p["group"])
+        self.lb = lb
+        self.g_coh = np.asarray(p["g_coh"], np.float32).reshape(lb.nc, lb.nc)
+        self.g_adh = np.asarray(p["gadh"] if p["gadh"] is not None else np.zeros(lb.nc), np.float32).reshape(-1)
+        self.psi1, self.psi2 = p["psi_list"][0], p["psi_list"][1]
+        self.fluid_strategy = p["fluid_strategy"]
+        fn = self.fluid_strategy or (lambda i, j: True)
+        sel = evaluate_predicate(fn, lb.NX + 2, lb.NY + 2, -1, -1)
+        fluid = np.zeros((lb.NY + 2, lb.psi_pitch), np.uint8)
+        fluid[:, :lb.NX + 2] = sel.T
+        self._fluid = torch.as_tensor(fluid, device=lb.device)
+
+    def mc_struct(self):
+        s = _capi.LbmMCShanChen()
+        nc = self.lb.nc
+        for a in range(nc):
+            for b in range(nc):
+                s.g_coh[a][b] = float(self.g_coh[a, b])
+            s.g_adh[a] = float(self.g_adh[a]) if a < self.g_adh.size else 0.0
+        s.eos[0] = self.psi1.struct()
+        s.eos[1] = self.psi2.struct()
+        s.fluid = self._fluid.data_ptr()
+        return s
+
+    def _call(self, fn, lb_field):
+        L = lb_field._mclattice()
+        _capi.call(fn, ctypes.byref(L), ctypes.byref(self.mc_struct()), self.group.on(lb_field).ptr,
+                   self.group.n, stream_handle())
+
+    def update_psi(self, lb_field):
+        """ExternalForce.py:86-92"""
+        self._call("lbm_mc_update_psi", lb_field)
+
+    def cau_SCforce(self, lb_field):
+        """ExternalForce.py:96-117"""
+        self._call("lbm_mc_sc_force", lb_field)
 
 
 # ------------------------------------------------------------ psi boundaries
+def _psi_periodic(lb_field, axis):
+    if lb_field.nc > 1:
+        L = lb_field._mclattice()
+        _capi.call("lbm_mc_psi_periodic", ctypes.byref(L), axis, stream_handle())
+    else:
+        L = lb_field._lattice()
+        _capi.call("lbm_psi_periodic", ctypes.byref(L), axis, stream_handle())
+
+
 class PeriodicPsi_LR:
-    """SCBoundaryCondition.py:126-134"""
+    """SCBoundaryCondition.py:126-134 (every component)"""
 
     def apply(self, lb_field):
-        L = lb_field._lattice()
-        _capi.call("lbm_psi_periodic", ctypes.byref(L), 0, stream_handle())
+        _psi_periodic(lb_field, 0)
 
 
 class PeriodicPsi_BT:
-    """SCBoundaryCondition.py:136-144"""
+    """SCBoundaryCondition.py:136-144 (every component)"""
 
     def apply(self, lb_field):
-        L = lb_field._lattice()
-        _capi.call("lbm_psi_periodic", ctypes.byref(L), 1, stream_handle())
+        _psi_periodic(lb_field, 1)
 
 
 class FixedPsi(BoundaryCondition):

@@ -54,6 +54,9 @@ class FusedSolver:
                  nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
                  sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True, lane_special=True,
                  fixed_exp=None, wait_cycles=0):
+        if lb_field.nc > 1:
+            raise UnsupportedComposition("the fused step is single-component; a multi-component lattice "
+                                         "runs the per-stage kernels")
         self.sc = lb_field.sc_field
         # fixed-point storage: step 2^-fixed_exp, range |f - w rho_ref| < 2^(15 - fixed_exp)
         self.fixed_exp = int(fixed_exp) if fixed_exp is not None else A.FIXED_EXP_DEFAULT
