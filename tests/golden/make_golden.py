@@ -325,7 +325,8 @@ def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bg
             ob.precompute(classifier=cls_psi)
             name = f"psi_{kind}_{n_}"
             bsc.add_boundary_condition(name, ob)
-            case.meta["psi_bcs"].append({"kind": kind, "name": name, "direction": int(direction)})
+            case.meta["psi_bcs"].append({"kind": kind, "name": name, "direction": int(direction),
+                                         "row": int(row)})
             case.groups["g_" + name] = np.asarray(sorted(map(tuple, group_nodes(ob.group))),
                                                   np.int32).reshape(-1, 2)
     else:
@@ -340,7 +341,7 @@ def build_shanchen(ti, tl, case, nx, ny, *, eos, g_coh, rho_init, collision=("bg
         fp = tl.FixedPsi(spec=tl.BoundarySpec(geometry_fn=row_fn), psi_value=value)
         fp.precompute(classifier=cls)
         bsc.add_boundary_condition("fixed", fp)
-        case.meta["psi_bcs"].append({"kind": "fixed", "name": "psi_fixed", "value": float(value)})
+        case.meta["psi_bcs"].append({"kind": "fixed", "name": "psi_fixed", "value": float(value), "row": int(row)})
         case.groups["g_psi_fixed"] = np.asarray(sorted(map(tuple, group_nodes(fp.group))), np.int32).reshape(-1, 2)
 
     lb.T.fill(T)

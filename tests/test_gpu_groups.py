@@ -81,6 +81,18 @@ def classify(tl, meta):
             fn = preds[name]
         g = cls.get_group(tl.BoundarySpec(geometry_fn=fn))
         groups["g_" + name] = g.nodes
+    # psi boundaries: FixedPsi on a lattice row, the open psi boundaries on
+    # a row of the psi grid (-1..NX, -1..NY), nodes 0 <= i < NX
+    psi_cls = tl.BoundaryClassifier((nx + 2, ny + 2), offset=(-1, -1))
+    for pb in meta.get("psi_bcs", []):
+        if not isinstance(pb, dict):
+            continue
+        row = pb["row"]
+        if pb["kind"] == "fixed":
+            g = cls.get_group(tl.BoundarySpec(geometry_fn=lambda i, j, r=row: (lb.mask[i, j] == 1) & (j == r)))
+        else:
+            g = psi_cls.get_group(tl.BoundarySpec(geometry_fn=lambda i, j, r=row: (j == r) & (i >= 0) & (i < nx)))
+        groups["g_" + pb["name"]] = g.nodes
     return mask, groups
 
 
