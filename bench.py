@@ -61,6 +61,11 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched Shan-Chen lines")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--requests", type=int, default=64, help="requests in the served stream")
+    ap.add_argument("--served-capacity", type=float, default=None, metavar="MLUPS",
+                    help="capacity the served stream's arrival rate is 80%% of (default: the single-lattice "
+                         "BGK fp16s line)")
+    ap.add_argument("--alone-sample", type=int, default=16,
+                    help="served requests also run alone on the plain fp32 path, as the baseline")
     ap.add_argument("--mix-only", type=int, default=0, metavar="N",
                     help="only time the batched step of the first N served requests (all packed)")
     ap.add_argument("--mix-v", type=int, default=None, help="nodes per thread of the --mix-only members")
@@ -463,15 +468,15 @@ def run_ours(a):
             "fp32": run_batched(tl, "fp32", kb, W, local),
             "fp16s": run_batched(tl, "fp16s", kb, W, local)}
     if not a.no_served and ws == 1:
-        cap = line.get("models", {}).get("bgk_fp16s", {}).get("MLUPS", 100000.0)
+        cap = a.served_capacity or line.get("models", {}).get("bgk_fp16s", {}).get("MLUPS", 100000.0)
         line["served"] = dict(
             {"workload": f"{a.requests} cylinder-channel requests (seed 20261203): NX in {{128, 160, ..., "
                          "2048}, NY = NX/4, r = NY/10 at x = NX/5, Re ~ U[20, 200] via tau (u_max 0.04), "
                          "steps log-uniform in [2000, 50000], BGK/TRT/MRT uniform, 20% power law n ~ "
-                         "U[0.5, 1.5]; Poisson arrivals at 80% of the capacity implied by the single-lattice "
-                         f"BGK fp16s MLUPS; {a.served_storage} storage, HBM budget 64 GiB, 200-step slices, "
+                         f"U[0.5, 1.5]; Poisson arrivals at 80% of a capacity of {cap:.0f} MLUPS; "
+                         f"{a.served_storage} storage, HBM budget 64 GiB, 200-step slices, "
                          "CUDA graphs; diverged requests are evicted and their updates not counted"},
-            **run_served(tl, a.requests, cap, local, storage=a.served_storage))
+            **run_served(tl, a.requests, cap, local, storage=a.served_storage, sample_alone=a.alone_sample))
     if rank == 0 and ws == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(cfg, a.model, a.cpu_seconds)
     if dist is not None:
