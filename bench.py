@@ -6,7 +6,8 @@ A "step" is one lattice-Boltzmann time step over the whole lattice.
   value  : lattice updates/s with the state resident in HBM (K fused steps)
   e2e    : the same through the drop-in API from host buffers: upload rho/u,
            init_LBM, FusedSolver.step(K), read rho/u back
-  models : the other collision models and the 16-bit storages, same lattice
+  models : the other collision models and the 16-bit storages, same lattice; BGK fp32 and fp16s
+           also in place (one population buffer, the AA pattern)
   batched: 64 periodic Shan-Chen lattices of uneven sizes in one Batch
   served : a Poisson stream of cylinder-channel requests through a Server,
            with p50/p99 latency, beside the same requests run alone in fp32
@@ -201,12 +202,13 @@ def barrier(dist):
         torch.cuda.synchronize()
 
 
-def build(tl, cfg, model, storage, V, pipeline="direct"):
+def build(tl, cfg, model, storage, V, pipeline="direct", in_place=False):
     from taichi_lbm.workloads import cylinder_channel
     lb, me, coll, be = cylinder_channel(tl, cfg["nx"], cfg["ny"], cfg["radius"], cfg["cx"], cfg["cy"],
                                         cfg["tau"], cfg["umax"], model=model,
                                         mrt_s=MRT_S if model == "mrt" else None, keep_init=False)
-    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, nodes_per_thread=V, pipeline=pipeline)
+    solver = tl.FusedSolver(lb, me, coll, be, storage=storage, nodes_per_thread=V, pipeline=pipeline,
+                            in_place=in_place)
     return lb, me, coll, be, solver
 
 
@@ -443,15 +445,18 @@ def run_ours(a):
     torch.cuda.empty_cache()
     if not a.no_extras and ws == 1:
         extras = {}
-        for model, storage in (("trt", "fp32"), ("mrt", "fp32"), ("bgk", "fp16s"), ("bgk", "bf16s"), ("bgk", "i16s")):
-            if (model, storage) == (a.model, a.storage):
+        for model, storage, aa in (("trt", "fp32", False), ("mrt", "fp32", False), ("bgk", "fp16s", False),
+                                   ("bgk", "bf16s", False), ("bgk", "i16s", False), ("bgk", "fp32", True),
+                                   ("bgk", "fp16s", True)):
+            if (model, storage, aa) == (a.model, a.storage, False) or (aa and a.pipeline != "direct"):
                 continue
-            lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None, a.pipeline)
+            lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None, a.pipeline, in_place=aa)
             k2 = max(10, K // 4)
             ms2, _ = time_resident(s2, k2, W, None, local)
             act = coll2.group.n
             gbs = BYTES_PER_LU[storage] * act / (ms2 / k2 * 1e-3) / 1e9
-            extras[f"{model}_{storage}"] = {"MLUPS": round(act * k2 / (ms2 * 1e-3) / 1e6, 1),
+            extras[f"{model}_{storage}" + ("_in_place" if aa else "")] = {
+                                            "MLUPS": round(act * k2 / (ms2 * 1e-3) / 1e6, 1),
                                             "GB_s": round(gbs, 1), "frac": round(gbs / peak, 4),
                                             "steps": k2}
             del s2, lb2, coll2

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define LBM_GB300_ABI_VERSION 3
+#define LBM_GB300_ABI_VERSION 4
 
 enum {
   LBM_OK = 0,
@@ -357,6 +357,19 @@ typedef struct LbmPlanDesc {
    * the copies still in flight are then waited for with the default budget
    * before the kernel returns.                                             */
   int64_t wait_cycles;
+  /* 1 = in-place (AA-pattern) step: ONE population buffer (bind fa == fb)
+   * instead of the ping-pong pair.  Steps alternate two phases whose nodes
+   * each read and write the same nine locations: phase A gathers as the
+   * pull step does and writes f*_opp(k)(x) where it read f_k(x); phase B
+   * reads f_k(x) from slot opp(k) of x and writes f*_k(x) to slot k of x.
+   * A run that ends on phase A swaps the streamed pairs back, so between
+   * runs the buffer holds what the ping-pong state would hold, bit for bit.
+   * Needs the direct pipeline, no Shan-Chen, the lane-granular lists, every
+   * bounce-back link cut on both sides (a colliding node that bounces back
+   * the population coming from a colliding neighbour is bounced back by it
+   * too), no colliding node streaming from a node outside the collision
+   * group, and the boundary read sites (LbmPlanBuffers.aa_sites).          */
+  int32_t aa;
 } LbmPlanDesc;
 
 #define LBM_FIXED_EXP_DEFAULT 19
@@ -421,13 +434,25 @@ typedef struct LbmPlanBuffers {
   const uint32_t* lane_mask;
   const int32_t* lanes;
   int32_t nlanes;
+  /* In-place step (LbmPlanDesc.aa): the plane offsets y * pitch + x of every
+   * node whose post-stream populations a boundary program reads (the
+   * neighbours x - c_dir of VelocityNEEM, PressureNEEM, OpenNeumann and
+   * OpenConvective1order nodes, and x - c_dir, x - 2 c_dir of
+   * OpenExtrapolation nodes), ascending and distinct, and aa_vals, device
+   * scratch of 9 * aa_nsites floats.  Each step gathers those populations
+   * into aa_vals before it overwrites them.  Required when a program reads
+   * neighbours; ignored by the ping-pong step.                             */
+  const int32_t* aa_sites;
+  int32_t aa_nsites;
+  float* aa_vals;
 } LbmPlanBuffers;
 
 typedef struct LbmPlan LbmPlan;
 
 int lbm_plan_create(const LbmPlanDesc* desc, LbmPlan** out);
 int lbm_plan_bind(LbmPlan* plan, const LbmPlanBuffers* bufs);
-/* Launch nsteps fused steps, alternating fa/fb and mom_a/mom_b. */
+/* Launch nsteps fused steps, alternating fa/fb and mom_a/mom_b (in place:
+ * phases A and B on fa, then the swap back after an odd count). */
 int lbm_plan_run(LbmPlan* plan, int32_t nsteps, void* stream);
 /* Which buffer holds the current post-collision state: 0 = fa/mom_a, 1 = fb/mom_b. */
 int lbm_plan_get_parity(const LbmPlan* plan, int32_t* parity);

@@ -1,0 +1,3 @@
+// In-place (AA-pattern) step kernels with fp16 (shifted) population storage.
+#include "lbm_fused_aa.cuh"
+LBM_AA_INSTANTIATE(LBM_STORE_F16S, 4, 8)

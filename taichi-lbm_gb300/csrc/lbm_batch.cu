@@ -155,7 +155,10 @@ int batch_step(LbmBatch* b, int sp, cudaStream_t s) {
   if (rc) return rc;
   int rl = LBM_OK;
   int k = 0;
-  for (size_t i = 0; i < b->groups.size() && !rl; ++i)
+  // the small, latency-bound groups (marked lanes, power-law segments) are
+  // launched first, so their blocks are spread over the SMs beside the big
+  // plain group instead of running alone after it
+  for (size_t i = b->groups.size(); i-- > 0 && !rl;)
     rl = launch_group(b->groups[i], b->d_lats, b->d_tiles, sp, b->work[k++ % nw]);
   for (size_t i = 0; i < b->solos.size() && !rl; ++i) {
     const LbmBatch::Solo& m = b->solos[i];
@@ -326,8 +329,8 @@ int rebuild(LbmBatch* b) {
       mons[pl->d.storage].push_back(bm);
     }
   }
-  // plain groups first (the bulk of the work), then Shan-Chen, then flagged:
-  // the key order starts with the kind
+  // groups in key order (the kind first: plain, Shan-Chen, flagged); a step
+  // launches them in the reverse order
   std::vector<std::pair<GroupKey, std::vector<BatchTile>>> buckets(by_key.begin(), by_key.end());
   std::vector<BatchTile> tiles;
   b->groups.clear();
@@ -463,6 +466,7 @@ int lbm_batch_add(LbmBatch* b, LbmPlan* plan, const uint32_t* host_lane_mask, in
   if (!plan->bound) return lbm_err::set(LBM_ERR_STATE, "batch_add: plan not bound");
   const LbmPlanDesc& d = plan->d;
   const int V = d.nodes_per_thread;
+  if (d.aa) return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch_add: batched members run the ping-pong step");
   if (d.sc && V != lbm::AV)
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "batch_add: Shan-Chen members run %d nodes per lane", lbm::AV);
   if (d.storage == LBM_STORE_F32 ? (V != 2 && V != 4) : (V != 4 && V != 8))

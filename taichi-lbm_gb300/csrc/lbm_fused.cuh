@@ -74,7 +74,17 @@ struct FusedParams {
   int32_t* status;
   // LBM_PIPE_ASYNC: clock-cycle budget of each wait on a staged copy
   long long wait_cycles;
+  // in-place AA-pattern step (lbm_fused_aa.cuh): the phase of the running
+  // launch (0 outside an AA step, AA_PHASE_A / AA_PHASE_B), and the
+  // post-stream populations of the nodes boundary programs read
+  // (aa_vals[s * 9 + k] for the node at plane offset aa_sites[s], ascending),
+  // gathered before the step overwrites them
+  int aa;
+  const int32_t* aa_sites;
+  int aa_nsites;
+  float* aa_vals;
 };
+constexpr int AA_PHASE_A = 1, AA_PHASE_B = 2;
 
 // The fields the lean (plain-segment) kernels read: a compact copy of
 // FusedParams that a batched kernel can stage per warp in shared memory.
@@ -392,6 +402,27 @@ __device__ __forceinline__ void gather_node(const FusedParams& p, int x, int y, 
   }
 }
 
+// Post-stream populations of node (x, y) that a boundary program reads.  An
+// in-place AA step overwrites them while it runs, so it gathers them into
+// p.aa_vals first and a program looks them up there (binary search of the
+// node's plane offset); every other step pulls them from its source.
+template <int ST>
+__device__ __forceinline__ void read_site(const FusedParams& p, int x, int y, float g[9]) {
+  if (!p.aa) {
+    gather_node<ST>(p, x, y, g);
+    return;
+  }
+  const int q = y * p.pitch + x;
+  int lo = 0, hi = p.aa_nsites - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (p.aa_sites[mid] < q) lo = mid + 1;
+    else hi = mid;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) g[k] = p.aa_nsites > 0 ? p.aa_vals[(size_t)lo * 9 + k] : 0.0f;
+}
+
 __device__ __forceinline__ float bc_rhow(int dir, float vx, float vy, const float f[9]) {
   // BoundaryCondition.py:119-129
   if (dir == 2) return 1.0f / (1.0f + vy) * (f[0] + f[1] + f[3] + 2.0f * (f[2] + f[5] + f[6]));
@@ -428,7 +459,7 @@ __device__ __noinline__ void apply_bc(const FusedParams& p, int bci, int x, int 
     case LBM_BC_VELOCITY_NEEM: {  // BoundaryCondition.py:154-166
       const float r = bc_rhow(dir, Ux, Uy, f), uu = Ux * Ux + Uy * Uy;
       float g[9];
-      gather_node<ST>(p, x2, y2, g);
+      read_site<ST>(p, x2, y2, g);
       const float r2 = p.mom_in[q2], u2x = p.mom_in[p.plane + q2], u2y = p.mom_in[2 * p.plane + q2];
       const float uu2 = u2x * u2x + u2y * u2y;
 #pragma unroll
@@ -456,7 +487,7 @@ __device__ __noinline__ void apply_bc(const FusedParams& p, int bci, int x, int 
     }
     case LBM_BC_PRESSURE_NEEM: {  // BoundaryCondition.py:215-226
       float g[9];
-      gather_node<ST>(p, x2, y2, g);
+      read_site<ST>(p, x2, y2, g);
       const float r = p.mom_in[q], r2 = p.mom_in[q2];
       const float ux = p.mom_in[p.plane + q2], uy = p.mom_in[2 * p.plane + q2];
       const float uu = ux * ux + uy * uy;
@@ -468,7 +499,7 @@ __device__ __noinline__ void apply_bc(const FusedParams& p, int bci, int x, int 
     case LBM_BC_OPEN_NEUMANN:  // BoundaryCondition.py:321-334
     case LBM_BC_OPEN_CONV1: {  // BoundaryCondition.py:342-359
       float g[9];
-      gather_node<ST>(p, x2, y2, g);
+      read_site<ST>(p, x2, y2, g);
       float lam = 0.0f;
       if (b.kind == LBM_BC_OPEN_CONV1) {
         const float ux = p.mom_in[p.plane + q2], uy = p.mom_in[2 * p.plane + q2];
@@ -481,8 +512,8 @@ __device__ __noinline__ void apply_bc(const FusedParams& p, int bci, int x, int 
     }
     case LBM_BC_OPEN_EXTRAP: {  // BoundaryCondition.py:400-411
       float g2[9], g3[9];
-      gather_node<ST>(p, x2, y2, g2);
-      gather_node<ST>(p, x2 - cx_dyn(dir), y2 - cy_dyn(dir), g3);
+      read_site<ST>(p, x2, y2, g2);
+      read_site<ST>(p, x2 - cx_dyn(dir), y2 - cy_dyn(dir), g3);
 #pragma unroll
       for (int k = 1; k < 9; ++k)
         if (is_unknown_dyn(dir, k)) f[k] = 2.0f * g2[k] - g3[k];

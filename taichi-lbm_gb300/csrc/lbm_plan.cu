@@ -4,6 +4,7 @@
 #include <mutex>
 #include <new>
 
+#include "lbm_fused_aa.cuh"
 #include "lbm_fused_launch.cuh"
 #include "lbm_plan_internal.h"
 
@@ -11,6 +12,10 @@ LBM_EXTERN_STORAGE(LBM_STORE_F32)
 LBM_EXTERN_STORAGE(LBM_STORE_F16S)
 LBM_EXTERN_STORAGE(LBM_STORE_BF16S)
 LBM_EXTERN_STORAGE(LBM_STORE_I16S)
+LBM_AA_EXTERN(LBM_STORE_F32)
+LBM_AA_EXTERN(LBM_STORE_F16S)
+LBM_AA_EXTERN(LBM_STORE_BF16S)
+LBM_AA_EXTERN(LBM_STORE_I16S)
 
 namespace {
 
@@ -128,6 +133,82 @@ int step_once(LbmPlan* pl, cudaStream_t s) {
   return LBM_OK;
 }
 
+// one in-place step of the given phase on stream s: the boundary read sites,
+// then the marked lanes (side stream) and the plain segments, joined
+int aa_step(LbmPlan* pl, int phase, cudaStream_t s) {
+  FusedParams p = params_for(pl);
+  p.aa = phase;
+  p.aa_sites = pl->b.aa_sites;
+  p.aa_nsites = pl->b.aa_nsites;
+  p.aa_vals = pl->b.aa_vals;
+  const int st = pl->d.storage;
+  int rc = st == LBM_STORE_F32    ? lbm::launch_aa_sites<LBM_STORE_F32>(p, s)
+           : st == LBM_STORE_F16S ? lbm::launch_aa_sites<LBM_STORE_F16S>(p, s)
+           : st == LBM_STORE_BF16S ? lbm::launch_aa_sites<LBM_STORE_BF16S>(p, s)
+                                   : lbm::launch_aa_sites<LBM_STORE_I16S>(p, s);
+  if (rc) return rc;
+  const bool fork = p.nlanes > 0 && pl->b.special_stream;
+  cudaStream_t s2 = s;
+  if (fork) {
+    rc = ensure_side(pl);
+    if (rc) return rc;
+    s2 = pl->side;
+    rc = lbm_err::cuda(cudaEventRecord(pl->fork, s), "plan_run: fork");
+    if (!rc) rc = lbm_err::cuda(cudaStreamWaitEvent(s2, pl->fork, 0), "plan_run: fork");
+    if (rc) return rc;
+  }
+  const int V = pl->d.nodes_per_thread;
+  rc = st == LBM_STORE_F32    ? lbm::launch_aa<LBM_STORE_F32>(p, V, s, s2)
+       : st == LBM_STORE_F16S ? lbm::launch_aa<LBM_STORE_F16S>(p, V, s, s2)
+       : st == LBM_STORE_BF16S ? lbm::launch_aa<LBM_STORE_BF16S>(p, V, s, s2)
+                               : lbm::launch_aa<LBM_STORE_I16S>(p, V, s, s2);
+  if (fork) {
+    int rj = lbm_err::cuda(cudaEventRecord(pl->join, s2), "plan_run: join");
+    if (!rj) rj = lbm_err::cuda(cudaStreamWaitEvent(s, pl->join, 0), "plan_run: join");
+    if (!rc) rc = rj;
+  }
+  if (rc) return rc;
+  pl->parity ^= 1;
+  return LBM_OK;
+}
+
+// back to pull layout after a run that ended on phase A
+int aa_swap(LbmPlan* pl, cudaStream_t s) {
+  const FusedParams p = params_for(pl);
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return lbm::launch_aa_swap<LBM_STORE_F32>(p, s);
+    case LBM_STORE_F16S: return lbm::launch_aa_swap<LBM_STORE_F16S>(p, s);
+    case LBM_STORE_BF16S: return lbm::launch_aa_swap<LBM_STORE_BF16S>(p, s);
+    default: return lbm::launch_aa_swap<LBM_STORE_I16S>(p, s);
+  }
+}
+
+int mex(LbmPlan* pl, const int32_t* links, int64_t n, double* out, cudaStream_t s) {
+  FusedParams p = params_for(pl);
+  switch (pl->d.storage) {
+    case LBM_STORE_F32: return lbm::launch_momentum_exchange<LBM_STORE_F32>(p, links, n, out, s);
+    case LBM_STORE_F16S: return lbm::launch_momentum_exchange<LBM_STORE_F16S>(p, links, n, out, s);
+    case LBM_STORE_BF16S: return lbm::launch_momentum_exchange<LBM_STORE_BF16S>(p, links, n, out, s);
+    default: return lbm::launch_momentum_exchange<LBM_STORE_I16S>(p, links, n, out, s);
+  }
+}
+
+// nsteps steps (ping-pong or in place), each followed by the momentum
+// exchange into series[2 * step] when series is given.  An in-place run
+// alternates phases A and B from A and ends in pull layout.
+int run_steps(LbmPlan* pl, int32_t nsteps, const int32_t* links, int64_t n, double* series, cudaStream_t s) {
+  for (int32_t st = 0; st < nsteps; ++st) {
+    int rc = pl->d.aa ? aa_step(pl, (st & 1) ? lbm::AA_PHASE_B : lbm::AA_PHASE_A, s) : step_once(pl, s);
+    if (rc) return rc;
+    if (series) {
+      rc = mex(pl, links, n, series + 2 * (size_t)st, s);
+      if (rc) return rc;
+    }
+  }
+  if (pl->d.aa && (nsteps & 1)) return aa_swap(pl, s);
+  return LBM_OK;
+}
+
 }  // namespace
 
 lbm::FusedParams lbm_plan_params(const LbmPlan* pl) { return params_for(pl); }
@@ -159,6 +240,9 @@ int lbm_plan_create(const LbmPlanDesc* d, LbmPlan** out) {
   if (d->wait_cycles < 0) return lbm_err::set(LBM_ERR_ARG, "wait_cycles %lld", (long long)d->wait_cycles);
   if (d->sc && d->storage == LBM_STORE_I16S)  // the strips' stores do not conserve a node's stored sum
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "Shan-Chen plans store fp32, fp16 or bf16 populations");
+  if (d->aa != 0 && d->aa != 1) return lbm_err::set(LBM_ERR_ARG, "aa %d (0 or 1)", d->aa);
+  if (d->aa && (d->pipeline != LBM_PIPE_DIRECT || d->sc))
+    return lbm_err::set(LBM_ERR_UNSUPPORTED, "the in-place step runs the direct pipeline without Shan-Chen");
   if (d->pipeline == LBM_PIPE_ASYNC && d->storage == LBM_STORE_I16S)
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "the fixed-point storage runs the direct or prefetch pipeline");
   if (d->pipeline == LBM_PIPE_ASYNC && (d->tune < 0 || d->tune >= LBM_ASYNC_TUNINGS))
@@ -267,6 +351,21 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
       !(b->special && b->plain))
     return lbm_err::set(LBM_ERR_UNSUPPORTED, "plan_bind: the prefetch pipeline at %d nodes per thread needs the "
                         "special and plain segment lists", pl->d.nodes_per_thread);
+  if (pl->d.aa) {
+    if (b->fa != b->fb) return lbm_err::set(LBM_ERR_ARG, "plan_bind: the in-place step needs fa == fb");
+    if (!b->special || !b->lane_mask || !b->lanes)
+      return lbm_err::set(LBM_ERR_ARG, "plan_bind: the in-place step needs the lane-granular lists (special, "
+                                       "lane_mask, lanes)");
+    bool reads = false;  // a boundary program reads a neighbour's populations
+    for (int i = 0; i < pl->d.nbc; ++i) {
+      const int k = pl->d.bc[i].kind;
+      reads = reads || k == LBM_BC_VELOCITY_NEEM || k == LBM_BC_PRESSURE_NEEM || k == LBM_BC_OPEN_NEUMANN ||
+              k == LBM_BC_OPEN_CONV1 || k == LBM_BC_OPEN_EXTRAP;
+    }
+    if (b->aa_nsites < 0 || (b->aa_nsites > 0 && (!b->aa_sites || !b->aa_vals)) || (reads && b->aa_nsites == 0))
+      return lbm_err::set(LBM_ERR_ARG, "plan_bind: %d boundary read sites for the in-place step%s", b->aa_nsites,
+                          reads ? " (its boundaries read neighbours: the sites are required)" : "");
+  }
   pl->b = *b;
   pl->bound = true;
   pl->parity = 0;
@@ -276,11 +375,7 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
 int lbm_plan_run(LbmPlan* pl, int32_t nsteps, void* stream) {
   if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "plan_run: plan not bound");
   if (nsteps < 0) return lbm_err::set(LBM_ERR_ARG, "plan_run: nsteps %d", nsteps);
-  for (int32_t s = 0; s < nsteps; ++s) {
-    int rc = step_once(pl, (cudaStream_t)stream);
-    if (rc) return rc;
-  }
-  return LBM_OK;
+  return run_steps(pl, nsteps, nullptr, 0, nullptr, (cudaStream_t)stream);
 }
 
 int lbm_plan_get_parity(const LbmPlan* pl, int32_t* parity) {
@@ -345,15 +440,6 @@ int lbm_plan_destroy(LbmPlan* pl) {
   return LBM_OK;
 }
 
-static int mex(LbmPlan* pl, const int32_t* links, int64_t n, double* out, cudaStream_t s) {
-  FusedParams p = params_for(pl);
-  switch (pl->d.storage) {
-    case LBM_STORE_F32: return lbm::launch_momentum_exchange<LBM_STORE_F32>(p, links, n, out, s);
-    case LBM_STORE_F16S: return lbm::launch_momentum_exchange<LBM_STORE_F16S>(p, links, n, out, s);
-    case LBM_STORE_BF16S: return lbm::launch_momentum_exchange<LBM_STORE_BF16S>(p, links, n, out, s);
-    default: return lbm::launch_momentum_exchange<LBM_STORE_I16S>(p, links, n, out, s);
-  }
-}
 
 int lbm_plan_momentum_exchange(LbmPlan* pl, const int32_t* links, int64_t n, double* out, void* stream) {
   if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "momentum_exchange: plan not bound");
@@ -366,14 +452,7 @@ int lbm_plan_run_monitored(LbmPlan* pl, int32_t nsteps, const int32_t* links, in
   if (!pl || !pl->bound) return lbm_err::set(LBM_ERR_STATE, "run_monitored: plan not bound");
   if (nsteps < 0 || !series || n < 0 || (n > 0 && !links))
     return lbm_err::set(LBM_ERR_ARG, "run_monitored: bad arguments");
-  cudaStream_t s = (cudaStream_t)stream;
-  for (int32_t st = 0; st < nsteps; ++st) {
-    int rc = step_once(pl, s);
-    if (rc) return rc;
-    rc = mex(pl, links, n, series + 2 * (size_t)st, s);
-    if (rc) return rc;
-  }
-  return LBM_OK;
+  return run_steps(pl, nsteps, links, n, series, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -86,7 +86,7 @@ class LbmPlanDesc(ctypes.Structure):
                 ("pipeline", ctypes.c_int32), ("tune", ctypes.c_int32),
                 ("sc", ctypes.c_int32), ("g_coh", ctypes.c_float), ("sc_T", ctypes.c_float),
                 ("eos", LbmEos), ("rho_ref", ctypes.c_float), ("fixed_exp", ctypes.c_int32),
-                ("wait_cycles", ctypes.c_int64)]
+                ("wait_cycles", ctypes.c_int64), ("aa", ctypes.c_int32)]
 
 
 # fixed-point storage step 2^-fixed_exp (range 2^(15 - fixed_exp))
@@ -106,7 +106,9 @@ class LbmPlanBuffers(ctypes.Structure):
                                                            ("special_stream", ctypes.c_int32),
                                                            ("plain", _vp), ("nplain", ctypes.c_int32),
                                                            ("lane_mask", _vp), ("lanes", _vp),
-                                                           ("nlanes", ctypes.c_int32)]
+                                                           ("nlanes", ctypes.c_int32),
+                                                           ("aa_sites", _vp), ("aa_nsites", ctypes.c_int32),
+                                                           ("aa_vals", _vp)]
 
 
 class LbmError(RuntimeError):
@@ -186,6 +188,9 @@ _SIGS = {
 EXPORTED = tuple(_SIGS)
 
 
+ABI_VERSION = 4
+
+
 def load():
     """Load the library (no CUDA call is made here)."""
     global _lib
@@ -199,6 +204,9 @@ def load():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
+    if lib.lbm_abi_version() != ABI_VERSION:  # the structs above follow this version of lbm_gb300.h
+        raise ImportError(f"{LIB_PATH} has ABI version {lib.lbm_abi_version()}, these bindings {ABI_VERSION}: "
+                          "rebuild it")
     _lib = lib
     return lib
 

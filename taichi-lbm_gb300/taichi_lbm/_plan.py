@@ -78,9 +78,11 @@ def _members(nx, ny, nodes):
     return m.reshape(nx, ny)
 
 
-def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
+def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread, in_place=False):
     """links: (nx, ny) int array, LBField.neighbor in bit form (bit k: link k
-    has a source; bit 15: node classified)."""
+    has a source; bit 15: node classified).  in_place: also check that the
+    in-place (AA-pattern) step can run the composition and list the nodes
+    whose post-stream populations boundary programs read (read_sites)."""
     V = int(nodes_per_thread)
     active = _members(nx, ny, np.asarray(collision_nodes, np.int32).reshape(-1, 2))
     carrier = np.full(nx * ny, -1, np.int32)  # flat views, scattered by linear index
@@ -281,13 +283,67 @@ def compile_plan(nx, ny, collision_nodes, links, items, nodes_per_thread):
     lane_mask = (lane_special.astype(np.uint64) * bits).sum(axis=2).astype(np.uint32)  # (ny, nseg)
     lanes = np.flatnonzero(lane_special.ravel()).astype(np.int32)  # (y * nseg + seg) * 32 + lane
 
+    read_sites = None
+    if in_place:
+        _check_in_place(code, active)
+        read_sites = _read_sites(items, rewrites, nx, ny)
+
     return CompiledPlan(code=code.astype(np.uint16), seg_flags=np.ascontiguousarray(seg_flags),
                         lane_mask=np.ascontiguousarray(lane_mask), lanes=lanes,
                         nseg=nseg, instances=instances, programs=programs, nprog=len(seqs) + 1,
                         bc_vel=bc_vel, items=items, active=active, save=save,
-                        n_special_segments=int(seg_flags.sum()))
+                        n_special_segments=int(seg_flags.sum()), read_sites=read_sites)
 
 
 def _prev_rewrite(rewrites, idx):
     pos = rewrites.index(idx)
     return rewrites[pos - 1] if pos > 0 else None
+
+
+OPP = np.array([0, 3, 4, 1, 2, 7, 8, 5, 6])
+
+
+def _check_in_place(code, active):
+    """The in-place step pairs the locations a node reads and writes; that
+    holds when every link cut by bounce-back is cut on both sides (node x
+    bounces back link k from a colliding source x - c_k only if that source
+    bounces back link opp(k) from x) and no colliding node streams from a
+    node outside the collision group.  Sources wrap around the lattice, as
+    the pull does."""
+    for k in range(1, 9):
+        shift = (int(CX[k]), int(CY[k]))
+        src_active = np.roll(active, shift, axis=(0, 1))  # active[x - c_k]
+        bounce = ((code >> (k - 1)) & 1).astype(bool)
+        src_bounce_back = np.roll(((code >> (OPP[k] - 1)) & 1).astype(bool), shift, axis=(0, 1))
+        one_sided = active & bounce & src_active & ~src_bounce_back
+        if one_sided.any():
+            i, j = np.argwhere(one_sided)[0]
+            raise UnsupportedComposition(
+                f"in-place step: node ({i}, {j}) bounces back link {k} from a colliding node that streams "
+                "the opposite link from it (a link cut on one side only)")
+        frozen = active & ~bounce & ~src_active
+        if frozen.any():
+            i, j = np.argwhere(frozen)[0]
+            raise UnsupportedComposition(
+                f"in-place step: node ({i}, {j}) streams link {k} from a node outside the collision group")
+
+
+def _read_sites(items, rewrites, nx, ny):
+    """(m, 2) int32 (x, y) of every node whose post-stream populations a
+    boundary program reads (x - c_dir, and x - 2 c_dir for extrapolation),
+    distinct and sorted by (y, x)."""
+    pts = []
+    for idx in rewrites:
+        it = items[idx]
+        if it.nodes.size == 0:
+            continue
+        _, _, x2_f, x3_f = READS[it.kind]
+        d = np.array([CX[it.direction], CY[it.direction]], np.int32)
+        if x2_f:
+            pts.append(it.nodes - d)
+        if x3_f:
+            pts.append(it.nodes - 2 * d)
+    if not pts:
+        return np.zeros((0, 2), np.int32)
+    q = np.unique(np.concatenate(pts).astype(np.int64) @ np.array([1, nx], np.int64))
+    return np.stack([q % nx, q // nx], 1).astype(np.int32)

@@ -14,6 +14,10 @@ and ``vel`` hold the moments of the final ``f``).  Internally: the first
 collision runs through the per-stage kernels, then n-1 fused launches (each
 = boundary pass of step k-1 + moments/collision of step k), then one stream
 and boundary pass and the moment kernels.
+
+``in_place=True`` runs the fused steps on one population buffer (the
+AA-pattern: alternating phases whose nodes read and write the same nine
+locations) instead of the ping-pong pair; the results are the same bits.
 """
 import ctypes
 import warnings
@@ -53,7 +57,7 @@ class FusedSolver:
     def __init__(self, lb_field, macroscopic_engine, collision, boundary_engine, storage="fp32",
                  nodes_per_thread=None, local_relaxation=None, pipeline="direct", tune=0,
                  sc_boundary_engine=None, two_pass=True, rho_ref=None, overlap=True, lane_special=True,
-                 fixed_exp=None, wait_cycles=0):
+                 fixed_exp=None, wait_cycles=0, in_place=False):
         if lb_field.nc > 1:
             raise UnsupportedComposition("the fused step is single-component; a multi-component lattice "
                                          "runs the per-stage kernels")
@@ -62,6 +66,12 @@ class FusedSolver:
         self.fixed_exp = int(fixed_exp) if fixed_exp is not None else A.FIXED_EXP_DEFAULT
         self.wait_cycles = int(wait_cycles)
         self.status_bits = 0
+        # in-place (AA-pattern) step: one population buffer instead of two
+        self.in_place = bool(in_place)
+        if self.in_place and (lb_field.sc_field is not None or pipeline != "direct" or not two_pass
+                              or not lane_special):
+            raise UnsupportedComposition("the in-place step runs the direct two-pass pipeline with "
+                                         "lane-granular special work, without Shan-Chen")
         self.lane_special = bool(lane_special)
         self.two_pass = bool(two_pass)
         self.overlap = bool(overlap)
@@ -135,7 +145,8 @@ class FusedSolver:
     def _build(self):
         lb, c = self.lb, self.coll
         nx, ny, P = lb.NX, lb.NY, lb.pitch
-        cp = compile_plan(nx, ny, self.group.nodes, lb.links_host(), boundary_items(self.be), self.V)
+        cp = compile_plan(nx, ny, self.group.nodes, lb.links_host(), boundary_items(self.be), self.V,
+                          in_place=self.in_place)
         self.compiled = cp
         dev = lb.device
         d = A.LbmPlanDesc()
@@ -209,6 +220,7 @@ class FusedSolver:
         d.rho_ref = self._rho_ref()
         d.fixed_exp = self.fixed_exp
         d.wait_cycles = self.wait_cycles
+        d.aa = 1 if self.in_place else 0
         self.desc = d
         # flagged segments, listed for the two-pass direct step
         flags = np.asarray(cp.seg_flags).ravel()
@@ -225,7 +237,15 @@ class FusedSolver:
         if self.storage == A.STORE_F32:
             self.fbuf = None
         else:
-            self.fbuf = [torch.zeros((9, ny, P), dtype=STATE_DTYPE[self.storage], device=dev) for _ in range(2)]
+            self.fbuf = [torch.zeros((9, ny, P), dtype=STATE_DTYPE[self.storage], device=dev)
+                         for _ in range(1 if self.in_place else 2)]
+        self.aa_sites = self.aa_vals = None
+        if self.in_place:
+            rs = cp.read_sites
+            q = (rs[:, 1].astype(np.int64) * P + rs[:, 0]).astype(np.int32)
+            self.aa_nsites = int(q.size)
+            self.aa_sites = torch.as_tensor(q if q.size else np.zeros(1, np.int32), device=dev)
+            self.aa_vals = torch.zeros(max(q.size, 1) * 9, dtype=torch.float32, device=dev)
         plan = ctypes.c_void_p()
         A.call("lbm_plan_create", ctypes.byref(d), ctypes.byref(plan))
         self._plan = plan
@@ -242,10 +262,11 @@ class FusedSolver:
     def _bind(self):
         lb = self.lb
         b = A.LbmPlanBuffers()
-        if self.fbuf is None:
-            b.fa, b.fb = lb._f2.data_ptr(), lb._f.data_ptr()
-        else:
-            b.fa, b.fb = self.fbuf[0].data_ptr(), self.fbuf[1].data_ptr()
+        bufs = self._state_buffers()
+        b.fa, b.fb = bufs[0].data_ptr(), bufs[-1].data_ptr()  # in place: one buffer, fa == fb
+        if self.in_place:
+            b.aa_sites, b.aa_nsites, b.aa_vals = (self.aa_sites.data_ptr(), self.aa_nsites,
+                                                  self.aa_vals.data_ptr())
         b.mom_a, b.mom_b = self.mom[0].data_ptr(), self.mom[1].data_ptr()
         b.code = self.code.data_ptr()
         b.seg_flags = self.seg_flags.data_ptr()
@@ -298,6 +319,8 @@ class FusedSolver:
     def launches_per_step(self):
         """Kernel launches of one lbm_plan_run step: two for the two-pass
         direct step (plain segments, then the listed ones), else one."""
+        if self.in_place:  # the boundary read sites, the marked lanes, the plain segments
+            return (1 if self.aa_nsites else 0) + (1 if self.nlanes else 0) + 1
         if (self.sc is None and self.pipeline in (A.PIPE_DIRECT, A.PIPE_PREFETCH) and self.two_pass
                 and self.nspecial and (self.nplain or self.pipeline == A.PIPE_DIRECT)):
             return 2
@@ -342,7 +365,7 @@ class FusedSolver:
             warnings.warn("fused run: a colliding node's populations became NaN or infinite (the flow "
                           "diverged)")
         if self.fbuf is None:
-            if par.value == 0:  # state in f2 -> write f
+            if par.value == 0 or self.in_place:  # state in f2 -> write f
                 A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f.data_ptr()), s)
             else:  # state in f's storage -> stream into f2's storage, then swap roles
                 A.call("lbm_plan_stream", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), s)
@@ -377,12 +400,14 @@ class FusedSolver:
         compiled node codes (geometry and boundary programs)."""
         d = self.desc
         return {"nx": int(d.nx), "ny": int(d.ny), "pitch": int(d.pitch), "storage": int(self.storage),
-                "model": int(d.model), "fluid_model": int(d.fluid_model), "sc": int(d.sc),
+                "model": int(d.model), "fluid_model": int(d.fluid_model), "sc": int(d.sc), "aa": int(d.aa),
                 "code_crc": zlib.crc32(np.ascontiguousarray(self.compiled.code).tobytes())}
 
     def _state_buffers(self):
-        # the two ping-pong buffers in bind order (fa, fb)
-        return list(self.fbuf) if self.fbuf is not None else [self.lb._f2, self.lb._f]
+        # the ping-pong buffers in bind order (fa, fb), or the in-place one
+        if self.fbuf is not None:
+            return list(self.fbuf)
+        return [self.lb._f2] if self.in_place else [self.lb._f2, self.lb._f]
 
     def checkpoint(self):
         """Snapshot of a live run (between begin() and finish()) as CPU tensors:

@@ -23,7 +23,7 @@ def test_library_exports_every_header_function(built):
     for n in names:
         assert hasattr(lib, n), f"{n} declared in lbm_gb300.h but not exported"
     assert set(names) == set(_capi.EXPORTED)
-    assert lib.lbm_abi_version() == 3
+    assert lib.lbm_abi_version() == 4
 
 
 def test_library_reports_argument_errors(built):
@@ -187,6 +187,45 @@ def test_plan_compiler_refusals():
                        BoundaryItem(A.BC_BOUNCEBACK, edge, name="w"), eq], 4)
     assert (cp.code[0, 0] & 0xFF) != 0 and (cp.code[3, 3] & 0xFF) == 0
 
+
+
+def test_plan_compiler_in_place_checks():
+    """The in-place step pairs each node's read and write locations: a link
+    cut by bounce-back on one side only, or a colliding node streaming from a
+    node outside the collision group, is refused; a channel walled on every
+    edge compiles and lists the nodes its NEEM outlet reads."""
+    from taichi_lbm import _capi as A
+    from taichi_lbm._plan import BoundaryItem, UnsupportedComposition, compile_plan
+    nx, ny = 8, 6
+    mask = np.ones((nx, ny), np.int32)
+    links = links_from_mask(mask)
+    allnodes = np.argwhere(mask == 1).astype(np.int32)
+    fl = BoundaryItem(A.BC_FLUID, allnodes, name="fluid")
+    per = BoundaryItem(A.BC_PERIODIC, allnodes, name="p")
+    bottom = allnodes[allnodes[:, 1] == 0]
+    # bottom row bounces back what the (periodic) top row streams to it
+    with pytest.raises(UnsupportedComposition, match="one side only"):
+        compile_plan(nx, ny, allnodes, links, [fl, per, BoundaryItem(A.BC_BOUNCEBACK, bottom, name="w")], 4,
+                     in_place=True)
+    # the same composition is fine for the ping-pong step
+    compile_plan(nx, ny, allnodes, links, [fl, per, BoundaryItem(A.BC_BOUNCEBACK, bottom, name="w")], 4)
+    # a colliding node streaming from a node outside the collision group
+    some = allnodes[allnodes[:, 0] != 3]
+    with pytest.raises(UnsupportedComposition, match="outside the collision group"):
+        compile_plan(nx, ny, some, links, [BoundaryItem(A.BC_FLUID, some, name="fluid"),
+                                           BoundaryItem(A.BC_PERIODIC, some, name="p")], 4, in_place=True)
+    # walls on every edge (both sides of every wrapped link cut) with a NEEM outlet
+    edge = allnodes[(allnodes[:, 0] == 0) | (allnodes[:, 0] == nx - 1) | (allnodes[:, 1] == 0)
+                    | (allnodes[:, 1] == ny - 1)]
+    outlet = allnodes[allnodes[:, 0] == nx - 1]
+    neem = BoundaryItem(A.BC_PRESSURE_NEEM, outlet, 1, 1.0, None, "out")
+    ext = BoundaryItem(A.BC_OPEN_EXTRAP, allnodes[allnodes[:, 0] == 0], 3, 0.0, None, "ext")
+    cp = compile_plan(nx, ny, allnodes, links, [fl, per, BoundaryItem(A.BC_BOUNCEBACK, edge, name="w"), neem, ext],
+                      4, in_place=True)
+    want = sorted({(nx - 2, j) for j in range(ny)} | {(1, j) for j in range(ny)} | {(2, j) for j in range(ny)},
+                  key=lambda t: (t[1], t[0]))
+    assert [tuple(t) for t in cp.read_sites.tolist()] == want
+    assert compile_plan(nx, ny, allnodes, links, [fl, per], 4, in_place=True).read_sites.shape == (0, 2)
 
 def test_segment_flags_mark_only_special_segments():
     from taichi_lbm import _capi as A
