@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--ny", type=int, default=CONFIG["ny"])
     ap.add_argument("--nodes-per-thread", type=int, default=None)
     ap.add_argument("--pipeline", default="direct", choices=["direct", "async"])
+    ap.add_argument("--in-place", action="store_true",
+                    help="headline lattice on the in-place (AA-pattern) step, one population buffer")
     ap.add_argument("--no-extras", action="store_true", help="skip the per-model/storage lines")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched Shan-Chen lines")
@@ -403,7 +405,8 @@ def run_ours(a):
     cfg = workload_config(a)
     K, W = a.steps, max(3, a.warmup)
     peak, peak_kind = measured_peak()
-    lb, me, coll, be, solver = build(tl, cfg, a.model, a.storage, a.nodes_per_thread, a.pipeline)
+    lb, me, coll, be, solver = build(tl, cfg, a.model, a.storage, a.nodes_per_thread, a.pipeline,
+                                     in_place=a.in_place)
     active = coll.group.n
     ms, clocks = time_resident(solver, K, W, dist, local)
     ms = max_over_ranks(ms, dist)
@@ -423,14 +426,18 @@ def run_ours(a):
                                f"parabolic inlet u_max={cfg['umax']}, PressureNEEM outlet, "
                                "bounce-back walls", "nodes": cfg["nx"] * cfg["ny"],
                    "updated_nodes_per_step": active, "model": a.model, "storage": a.storage,
-                   "nodes_per_thread": solver.V, "pipeline": a.pipeline,
+                   "nodes_per_thread": solver.V, "pipeline": a.pipeline, "in_place": a.in_place,
                    "parallelism": f"replicas x{ws}",
-                   "l2": "state (2 x 9 populations) larger than L2; no flush needed"},
+                   "l2": ("state (9 populations, one buffer)" if a.in_place else "state (2 x 9 populations)")
+                         + " larger than L2; no flush needed"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes_per_launch": BYTES_PER_LU[a.storage] * active,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel": ("one fused step: k_fused_bulk (every segment, marked lanes skipped) + k_fused_lanes "
+                     "kernel": ("one in-place step: k_aa_sites (boundary read sites), then k_aa_bulk (every "
+                                "segment, phases A and B alternating) + k_aa_lanes (marked lanes, side stream), "
+                                "timed together" if a.in_place else
+                                "one fused step: k_fused_bulk (every segment, marked lanes skipped) + k_fused_lanes "
                                 "(marked lanes, side stream), timed together"
                                 if solver.launches_per_step == 2 else "one fused step (one launch)")},
         "clocks": clocks,
@@ -448,7 +455,7 @@ def run_ours(a):
         for model, storage, aa in (("trt", "fp32", False), ("mrt", "fp32", False), ("bgk", "fp16s", False),
                                    ("bgk", "bf16s", False), ("bgk", "i16s", False), ("bgk", "fp32", True),
                                    ("bgk", "fp16s", True)):
-            if (model, storage, aa) == (a.model, a.storage, False) or (aa and a.pipeline != "direct"):
+            if (model, storage, aa) == (a.model, a.storage, a.in_place) or (aa and a.pipeline != "direct"):
                 continue
             lb2, _, coll2, _, s2 = build(tl, cfg, model, storage, None, a.pipeline, in_place=aa)
             k2 = max(10, K // 4)

@@ -255,20 +255,32 @@ struct Storage<LBM_STORE_I16S> {
 // Returns LBM_STATUS_SATURATED when a value left the range (or was NaN),
 // plus LBM_STATUS_NONFINITE when the node's values are NaN (a NaN in a
 // node's moments reaches all nine populations, so population 1 tells).
+// The range test is on the largest |h_k| (one max per value): below 32767.5
+// steps every value rounds into the int16 range, and only then are the
+// values stored unclamped; a value within half a step of -32768 steps also
+// takes the clamping path (and is reported), which stores the same bits.
 __device__ __forceinline__ int i16_conserve_bits(const float (&h)[9], float d, unsigned (&b)[9], float iq) {
   const unsigned mb = __float_as_uint(I16_MAGIC);
-  unsigned s = 0u;  // sum of the steps of populations 1..8 (two's complement)
-  bool out = false;
+  unsigned s = 0u;  // sum of the rounded bit patterns of populations 1..8
+  float m = 0.0f;   // largest |h_k| of populations 1..8
 #pragma unroll
   for (int k = 1; k < 9; ++k) {
-    const float r = fmaf(h[k], iq, I16_MAGIC);
-    const float t = fminf(fmaxf(r, I16_LO), I16_HI);
-    out = out || (t != r);  // clamped, or NaN (a NaN clamps to I16_LO)
-    b[k] = __float_as_uint(t);
-    s += b[k] - mb;
+    b[k] = __float_as_uint(fmaf(h[k], iq, I16_MAGIC));
+    s += b[k];
+    m = fmaxf(m, fabsf(h[k]));
   }
-  // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is exact
-  const int n0 = (int)(__float_as_uint(fmaf(d, iq, I16_MAGIC)) - mb) - (int)s;
+  const bool out = !(m * iq < 32767.5f) || h[1] != h[1];
+  if (out) {  // saturated or not finite: clamp (a NaN clamps to -32768)
+    s = 0u;
+#pragma unroll
+    for (int k = 1; k < 9; ++k) {
+      b[k] = __float_as_uint(fminf(fmaxf(fmaf(h[k], iq, I16_MAGIC), I16_LO), I16_HI));
+      s += b[k];
+    }
+  }
+  // d / Q is an integer of magnitude below 9 * 2^15, so d / Q + 1.5 * 2^23 is
+  // exact; the steps of populations 1..8 sum to s - 8 * bits(1.5 * 2^23)
+  const int n0 = (int)(__float_as_uint(fmaf(d, iq, I16_MAGIC)) - mb) - (int)(s - 8u * mb);
   b[0] = (unsigned)min(max(n0, -32768), 32767);
   const bool sat = out || n0 < -32768 || n0 > 32767;
   return (sat ? LBM_STATUS_SATURATED : 0) | (h[1] != h[1] ? LBM_STATUS_NONFINITE : 0);

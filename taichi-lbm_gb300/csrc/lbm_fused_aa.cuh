@@ -114,6 +114,26 @@ __device__ __forceinline__ void aa_collide_encode(const FusedParams& p, float (&
   }
 }
 
+// Elements [A, B) of v stored at p + A in aligned pieces of at most 16 B
+// (A, B known at compile time, p aligned to V elements).
+template <typename T, int A, int B>
+__host__ __device__ constexpr int store_piece() {
+  int n = 16 / (int)sizeof(T);
+  while (n > 1 && (A % n != 0 || A + n > B)) n /= 2;
+  return n;
+}
+template <typename T, int V, int A, int B>
+__device__ __forceinline__ void store_part(T* p, const T (&v)[V]) {
+  if constexpr (A < B) {
+    constexpr int n = store_piece<T, A, B>();
+    using R = typename Raw<n * (int)sizeof(T)>::type;
+    R r;
+    memcpy(&r, &v[A], sizeof(R));
+    *reinterpret_cast<R*>(p + A) = r;
+    store_part<T, V, A + n, B>(p, v);
+  }
+}
+
 // Phase A stores of one lane: node x writes population opp(k) to slot k of
 // x - c_k.  Along x that is a shift by one element, so the lane assembles the
 // aligned V elements [x0, x0 + V) of each row from its own nodes and one
@@ -163,8 +183,18 @@ __device__ __forceinline__ void aa_scatter(const FusedParams& p, const typename 
     bool all = live;
 #pragma unroll
     for (int i = 0; i < V; ++i) all = all && ok[i];
+    bool head = true, tail = true;  // elements 0..V-2 / 1..V-1 all stored here
+#pragma unroll
+    for (int i = 0; i < V - 1; ++i) {
+      head = head && ok[i];
+      tail = tail && ok[i + 1];
+    }
     if (all) {
       store_vec<T, V>(row + x0, v);
+    } else if (ST == LBM_STORE_F32 && live && head && !ok[V - 1]) {  // the last producer is another lane's
+      store_part<T, V, 0, V - 1>(row + x0, v);
+    } else if (ST == LBM_STORE_F32 && live && tail && !ok[0]) {  // the first producer is another lane's
+      store_part<T, V, 1, V>(row + x0, v);
     } else if (live) {
 #pragma unroll
       for (int i = 0; i < V; ++i)
