@@ -76,6 +76,9 @@ def parse():
                     help="lean kernel form of the --mix-only batch (lbm_batch_set_lean_form)")
     ap.add_argument("--mix-storage", default="i16s", choices=["fp16s", "bf16s", "i16s"],
                     help="storage of the --mix-only members")
+    ap.add_argument("--mix-solo", type=int, default=0, metavar="NODES",
+                    help="--mix-only members of at least NODES nodes run their own step (0: all packed)")
+    ap.add_argument("--mix-graphs", action="store_true", help="--mix-only batch replays CUDA graphs")
     ap.add_argument("--served-storage", default="i16s", choices=["fp32", "fp16s", "bf16s", "i16s"],
                     help="storage of the served requests")
     ap.add_argument("--batched-only", default=None, choices=["fp32", "fp16s", "bf16s"], metavar="STORAGE",
@@ -565,7 +568,7 @@ def run_mix(a):
     reqs = request_stream(a.mix_only, 20.0, storage=a.mix_storage)
     solvers = [r.build(tl, nodes_per_thread=a.mix_v) for r in reqs]
     nodes = sum(s.coll.group.n for s in solvers)
-    batch = tl.Batch(graphs=False, solo_nodes=0, lean_form=a.mix_form)
+    batch = tl.Batch(graphs=a.mix_graphs, solo_nodes=a.mix_solo, lean_form=a.mix_form)
     for s in solvers:
         batch.add(s)
     batch.run(a.warmup)
@@ -580,7 +583,10 @@ def run_mix(a):
     print(json.dumps({"metric": METRIC, "value": round(nodes / ms / 1e3, 1), "unit": METRIC, "steps": a.steps,
                       "warmup": a.warmup, "ms_per_step": round(ms, 4), "nodes": nodes, "info": batch.info(),
                       "config": {"workload": f"batched step of the first {a.mix_only} served requests (seed "
-                                             f"20261203), {a.mix_storage}, every member packed, direct launches",
+                                             f"20261203), {a.mix_storage}, "
+                                             + (f"members of at least {a.mix_solo} nodes solo" if a.mix_solo
+                                                else "every member packed")
+                                             + (", CUDA graphs" if a.mix_graphs else ", direct launches"),
                                  "nodes_per_thread": solvers[0].V, "lean_form": a.mix_form}}))
     batch.close()
 

@@ -461,7 +461,10 @@ int lbm_plan_set_parity(LbmPlan* plan, int32_t parity);
  * populations (fp32, [9][ny][pitch]) into f_out; moments are not computed.  */
 int lbm_plan_stream(LbmPlan* plan, float* f_out, void* stream);
 /* Convert fp32 populations into / out of the plan's current state buffer
- * (identity copies for fp32 storage, shifted 16-bit for F16S/BF16S).        */
+ * (identity copies for fp32 storage, shifted 16-bit for F16S/BF16S/I16S).
+ * Import writes both buffers: a step never writes a node outside the
+ * collision group, so fa and fb must hold the same populations there (a
+ * caller that fills the buffers itself keeps them equal at those nodes).    */
 int lbm_plan_import(LbmPlan* plan, const float* f_post, void* stream);
 int lbm_plan_export(LbmPlan* plan, float* f_post, void* stream);
 int lbm_plan_destroy(LbmPlan* plan);

@@ -805,7 +805,9 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
 
 // The general step of one node (x, row y) of a lane the lane mask marks,
 // from per-node gathers: what fused_tail does for a whole segment.  A node
-// outside the collision group keeps its stored values (copied bit for bit).
+// outside the collision group is not written: its populations never change,
+// and the plan's two buffers hold the same values there (lbm_plan_import
+// writes both).
 // One thread per node: the path is a chain of dependent loads (node code,
 // gathers, boundary reads), so nodes of a lane run side by side, not in turn.
 template <int MODEL, bool PL, int ST>
@@ -819,11 +821,7 @@ __device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
   {
     const size_t q = (size_t)y * p.pitch + x;
     const unsigned code = p.code[q];
-    if (!(code & LBM_CODE_ACTIVE)) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) dst[(size_t)k * p.plane + q] = load1(src + (size_t)k * p.plane + q);
-      return;
-    }
+    if (!(code & LBM_CODE_ACTIVE)) return;
     float f[9];
     gather_node<ST>(p, x, y, f);
     const unsigned prog = code >> LBM_CODE_PROG_SHIFT;

@@ -183,18 +183,8 @@ __device__ __forceinline__ void aa_scatter(const FusedParams& p, const typename 
     bool all = live;
 #pragma unroll
     for (int i = 0; i < V; ++i) all = all && ok[i];
-    bool head = true, tail = true;  // elements 0..V-2 / 1..V-1 all stored here
-#pragma unroll
-    for (int i = 0; i < V - 1; ++i) {
-      head = head && ok[i];
-      tail = tail && ok[i + 1];
-    }
     if (all) {
       store_vec<T, V>(row + x0, v);
-    } else if (ST == LBM_STORE_F32 && live && head && !ok[V - 1]) {  // the last producer is another lane's
-      store_part<T, V, 0, V - 1>(row + x0, v);
-    } else if (ST == LBM_STORE_F32 && live && tail && !ok[0]) {  // the first producer is another lane's
-      store_part<T, V, 1, V>(row + x0, v);
     } else if (live) {
 #pragma unroll
       for (int i = 0; i < V; ++i)
@@ -206,6 +196,43 @@ __device__ __forceinline__ void aa_scatter(const FusedParams& p, const typename 
 #pragma unroll
       for (int i = 0; i < V; ++i)
         if (i == ilast) row[0] = raw[i][o];  // node nx-1 -> column 0
+    }
+  }
+}
+
+// aa_scatter for an interior segment with no marked lane (x0s > 0,
+// x0s + 32 V < nx, mask 0): every producer is stored here, so only the
+// segment edges differ from a vector store per lane (16-bit storages: 7 %
+// faster in place than the general scatter)
+template <int ST, int V>
+__device__ __forceinline__ void aa_scatter_interior(const FusedParams& p, const typename Storage<ST>::T (&raw)[V][9],
+                                                    int y, int x0, int lane) {
+  using T = typename Storage<ST>::T;
+  constexpr unsigned FULL = 0xffffffffu;
+  T* dst = reinterpret_cast<T*>(p.dst);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int o = OPP(k);
+    T* row = dst + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch + x0;
+    T v[V];
+    if (CX(k) == 0) {
+#pragma unroll
+      for (int i = 0; i < V; ++i) v[i] = raw[i][o];
+      store_vec<T, V>(row, v);
+    } else if (CX(k) == 1) {  // element i <- node i + 1; node 0 -> x0 - 1
+      const T nxt = from_word<T>(__shfl_down_sync(FULL, to_word(raw[0][o]), 1));
+#pragma unroll
+      for (int i = 0; i < V; ++i) v[i] = i < V - 1 ? raw[i + 1 < V ? i + 1 : 0][o] : nxt;
+      if (lane < 31) store_vec<T, V>(row, v);
+      else store_part<T, V, 0, V - 1>(row, v);
+      if (lane == 0) row[-1] = raw[0][o];
+    } else {  // element i <- node i - 1; node V-1 -> x0 + V
+      const T prv = from_word<T>(__shfl_up_sync(FULL, to_word(raw[V - 1][o]), 1));
+#pragma unroll
+      for (int i = 0; i < V; ++i) v[i] = i > 0 ? raw[i > 0 ? i - 1 : 0][o] : prv;
+      if (lane > 0) store_vec<T, V>(row, v);
+      else store_part<T, V, 1, V>(row, v);
+      if (lane == 31) row[V] = raw[V - 1][o];
     }
   }
 }
@@ -229,7 +256,10 @@ __global__ void __launch_bounds__(256) k_aa_bulk(const FusedParams p) {
     if (mask == 0xffffffffu) return;  // uniform over the warp
     T raw[V][9];
     aa_collide_encode<MODEL, PL, ST, V, FORCE>(p, h, y, x0, !((mask >> lane) & 1u), raw);
-    aa_scatter<ST, V>(p, raw, y, x0, lane, mask);
+    // (fp32 takes the general scatter only: both forms inlined cost it 5 registers and more time)
+    if (ST != LBM_STORE_F32 && mask == 0u && x0s > 0 && x0s + 32 * V < p.nx)
+      aa_scatter_interior<ST, V>(p, raw, y, x0, lane);
+    else aa_scatter<ST, V>(p, raw, y, x0, lane, mask);
   } else {
     // f_k(x) is in slot opp(k) of x itself
     const T* src = reinterpret_cast<const T*>(p.src) + (size_t)y * p.pitch + x0;

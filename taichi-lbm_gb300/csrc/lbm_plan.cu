@@ -408,6 +408,21 @@ static int convert(LbmPlan* pl, const float* in, float* out, void* stream) {
   FusedParams p = params_for(pl);
   cudaStream_t s = (cudaStream_t)stream;
   void* cur = pl->parity ? pl->b.fb : pl->b.fa;
+  void* other = pl->parity ? pl->b.fa : pl->b.fb;
+  if (in && other != cur) {  // import: the other buffer too (nodes outside the group are never written)
+    int rc = LBM_OK;
+    switch (pl->d.storage) {
+      case LBM_STORE_F32:
+        if (in != other)
+          rc = lbm_err::cuda(cudaMemcpyAsync(other, in, 9 * p.plane * sizeof(float), cudaMemcpyDeviceToDevice, s),
+                             "import");
+        break;
+      case LBM_STORE_F16S: rc = lbm::launch_convert<LBM_STORE_F16S>(p, in, other, 1, s); break;
+      case LBM_STORE_BF16S: rc = lbm::launch_convert<LBM_STORE_BF16S>(p, in, other, 1, s); break;
+      default: rc = lbm::launch_convert<LBM_STORE_I16S>(p, in, other, 1, s); break;
+    }
+    if (rc) return rc;
+  }
   if (pl->d.storage == LBM_STORE_F32) {
     const size_t bytes = 9 * p.plane * sizeof(float);
     if (in && in != cur) return lbm_err::cuda(cudaMemcpyAsync(cur, in, bytes, cudaMemcpyDeviceToDevice, s), "import");

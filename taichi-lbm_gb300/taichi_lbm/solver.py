@@ -310,8 +310,10 @@ class FusedSolver:
         A.call("lbm_plan_set_parity", self._plan, 0)
         self.mom[0][0].copy_(lb._rho)
         self.mom[0][1:3].copy_(lb._vel)
-        if self.fbuf is not None:
+        if self.fbuf is not None:  # both buffers (a step never writes nodes outside the group)
             A.call("lbm_plan_import", self._plan, ctypes.c_void_p(lb._f2.data_ptr()), stream_handle())
+        elif not self.in_place:  # fp32: f2 is the state, f the other buffer; make them agree
+            lb._f.copy_(lb._f2)
         lb._fused_owner = self
         self._live = True
 
