@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--served-capacity", type=float, default=None, metavar="MLUPS",
                     help="capacity the served stream's arrival rate is 80%% of (default: the single-lattice "
                          "BGK fp16s line)")
+    ap.add_argument("--served-shape", default=None, metavar="V,SOLO,FORM",
+                    help="served batch shape (nodes per thread, solo threshold, lean form) instead of tuning it")
     ap.add_argument("--alone-sample", type=int, default=16,
                     help="served requests also run alone on the plain fp32 path, as the baseline")
     ap.add_argument("--mix-only", type=int, default=0, metavar="N",
@@ -320,7 +322,7 @@ def run_batched(tl, storage, K, W, gpu_index, graphs=True):
             "clocks": clk.summary()}
 
 
-def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8):
+def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8, shape=None):
     """Served request stream: n seeded cylinder-channel requests (sizes
     128..2048 x NX/4, Re 20..200, log-uniform 2k..50k steps, BGK/TRT/MRT, 20%
     power law) arriving as a Poisson process at 80% of the capacity implied by
@@ -334,12 +336,16 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
     mean_work = sum(r.nodes * r.steps for r in probe) / n
     rate = 0.8 * capacity_mlups * 1e6 / mean_work
     reqs = request_stream(n, rate, storage=storage)
-    # autotune (before the stream starts) in the batch itself, on the first 16
+    # autotune (before the stream starts) in the batch itself, on the first 32
     # requests: the members' nodes per thread and the solo threshold (a
     # lattice's fastest V alone is not its fastest in a packed mix)
     t0 = time.perf_counter()
     tuner = tl.Autotuner(steps=30, warmup=5)
-    tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=V) for r in reqs[:16]], storage)
+    if shape:  # given, not tuned
+        V, solo, form = (int(v) for v in shape.split(","))
+        tuner.table["served"] = {"V": V, "solo_nodes": solo, "sc_rows": 0, "lean_form": form, "given": True}
+    else:
+        tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=V) for r in reqs[:32]], storage)
     tune_s = time.perf_counter() - t0
     torch.cuda.empty_cache()
     srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=200, builders=4, autotuner=tuner)
@@ -369,7 +375,7 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
                                 "drag/lift, one after another",
                 "clocks": clk.summary(),
                 "autotune": {"seconds": round(tune_s, 1), "table": tuner.table,
-                             "what": "nodes per thread and solo threshold of the batch, tuned on the first 16 "
+                             "what": "nodes per thread and solo threshold of the batch, tuned on the first 32 "
                                      "requests, each candidate timed with CUDA events over 30 batched steps"}})
     out["vs_alone_fp32"] = round(out["MLUPS"] / out["alone_fp32_MLUPS"], 3)
     return out
@@ -491,7 +497,8 @@ def run_ours(a):
                          f"U[0.5, 1.5]; Poisson arrivals at 80% of a capacity of {cap:.0f} MLUPS; "
                          f"{a.served_storage} storage, HBM budget 64 GiB, 200-step slices, "
                          "CUDA graphs; diverged requests are evicted and their updates not counted"},
-            **run_served(tl, a.requests, cap, local, storage=a.served_storage, sample_alone=a.alone_sample))
+            **run_served(tl, a.requests, cap, local, storage=a.served_storage, sample_alone=a.alone_sample,
+                         shape=a.served_shape))
     if rank == 0 and ws == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(cfg, a.model, a.cpu_seconds)
     if dist is not None:

@@ -112,17 +112,8 @@ __host__ __device__ constexpr int lean_block_tiles(int form) {
   return BATCH_WARPS * (form == 1 ? LeanForm<1>::TPW : form == 2 ? LeanForm<2>::TPW : BATCH_TPW);
 }
 
-// Blocks per SM the pipelined kernel is compiled for: the Newtonian form 1
-// without a body force at 16 B of population per lane fits 64 registers
-// with a few bytes of spill, so four blocks (32 warps) stay resident; the
-// wider forms keep the compiler's own choice (0).
 template <bool PL, int ST, int V, int FORCE, int FORM>
-__host__ __device__ constexpr int lean_pf_min_blocks() {
-  return (!PL && !FORCE && FORM == 1 && (ST == LBM_STORE_F32 ? V == 2 : V == 4)) ? 4 : 0;
-}
-
-template <bool PL, int ST, int V, int FORCE, int FORM>
-__global__ void __launch_bounds__(BATCH_WARPS * 32, (lean_pf_min_blocks<PL, ST, V, FORCE, FORM>())) k_batch_lean_pf(const BatchLattice* __restrict__ lats,
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean_pf(const BatchLattice* __restrict__ lats,
                                                                      const BatchTile* __restrict__ tiles,
                                                                      int ntiles, int sp) {
   constexpr int NS = LeanForm<FORM>::NS, TPW = LeanForm<FORM>::TPW;
