@@ -155,10 +155,10 @@ int batch_step(LbmBatch* b, int sp, cudaStream_t s) {
   if (rc) return rc;
   int rl = LBM_OK;
   int k = 0;
-  // the small, latency-bound groups (marked lanes, power-law segments) are
-  // launched first, so their blocks are spread over the SMs beside the big
-  // plain group instead of running alone after it
-  for (size_t i = b->groups.size(); i-- > 0 && !rl;)
+  // in key order: the plain groups (the bulk of the work) first.  Launching
+  // the small groups first was measured: neutral on a fixed mix, but a
+  // served stream that packs its big lattices lost a third of its rate
+  for (size_t i = 0; i < b->groups.size() && !rl; ++i)
     rl = launch_group(b->groups[i], b->d_lats, b->d_tiles, sp, b->work[k++ % nw]);
   for (size_t i = 0; i < b->solos.size() && !rl; ++i) {
     const LbmBatch::Solo& m = b->solos[i];
@@ -329,8 +329,8 @@ int rebuild(LbmBatch* b) {
       mons[pl->d.storage].push_back(bm);
     }
   }
-  // groups in key order (the kind first: plain, Shan-Chen, flagged); a step
-  // launches them in the reverse order
+  // plain groups first (the bulk of the work), then Shan-Chen, then flagged:
+  // the key order starts with the kind
   std::vector<std::pair<GroupKey, std::vector<BatchTile>>> buckets(by_key.begin(), by_key.end());
   std::vector<BatchTile> tiles;
   b->groups.clear();

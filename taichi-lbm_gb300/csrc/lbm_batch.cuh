@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(MEX_TPB) k_batch_monitor(const BatchLattice* _
 
 // ------------------------------------------------------------ launchers
 // kind of a tile group
-enum { BATCH_LEAN = 0, BATCH_SC = 1, BATCH_SPECIAL = 2 };  // a step launches them in reverse
+enum { BATCH_LEAN = 0, BATCH_SC = 1, BATCH_SPECIAL = 2 };  // launch order within a step
 
 struct BatchGroup {
   int kind, model, powerlaw, storage, V, force;
