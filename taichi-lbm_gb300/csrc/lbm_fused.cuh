@@ -811,7 +811,7 @@ __device__ __forceinline__ void fused_tail(const FusedParams& p, float (&f)[V][9
 // One thread per node: the path is a chain of dependent loads (node code,
 // gathers, boundary reads), so nodes of a lane run side by side, not in turn.
 template <int MODEL, bool PL, int ST>
-__device__ __forceinline__ void lane_node(const FusedParams& p, int y, int x) {
+__device__ __forceinline__ void lane_node(const FusedParams& __restrict__ p, int y, int x) {
   using S = Storage<ST>;
   using T = typename S::T;
   const T* src = reinterpret_cast<const T*>(p.src);
