@@ -63,7 +63,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched Shan-Chen lines")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
-    ap.add_argument("--requests", type=int, default=64, help="requests in the served stream")
+    ap.add_argument("--requests", type=int, default=256,
+                    help="requests in the served stream (enough that the last requests' tail is a small part)")
     ap.add_argument("--served-capacity", type=float, default=None, metavar="MLUPS",
                     help="capacity the served stream's arrival rate is 80%% of (default: the single-lattice "
                          "BGK fp16s line)")
