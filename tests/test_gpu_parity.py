@@ -15,8 +15,12 @@ from tests.cases import (build_from_case, cylinder_channel, describe, fields_of,
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-5
-# power law: gamma^(n-1) amplifies last-bit differences of the strain rate
-TOL_PL = 5e-5
+# power law: the same 1e-5.  gamma^(n-1) amplifies last-bit differences of
+# the strain rate; where that lifts the fp32 reference's own distance from the
+# fp64 solution (the floor), check_parity allows 3x the floor, measured per case
+# (the u floor of the MRT n = 0.5 contraction is 1.1e-4, of the others 1.2e-5
+# to 1.5e-5)
+TOL_PL = 1e-5
 F64_CASES = {n for n in fixture_names() if n.endswith("_f64")}
 SC_CASES = {n for n in fixture_names() if n.startswith("sc_")}
 
