@@ -1,5 +1,6 @@
 // Fused-step plans: validation, buffer binding and stream-ordered launches.
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -353,6 +354,8 @@ int lbm_plan_bind(LbmPlan* pl, const LbmPlanBuffers* b) {
                         "special and plain segment lists", pl->d.nodes_per_thread);
   if (pl->d.aa) {
     if (b->fa != b->fb) return lbm_err::set(LBM_ERR_ARG, "plan_bind: the in-place step needs fa == fb");
+    if ((int64_t)pl->d.ny * pl->d.pitch > INT32_MAX)  // read sites are int32 plane offsets
+      return lbm_err::set(LBM_ERR_UNSUPPORTED, "plan_bind: the in-place step takes lattices below 2^31 sites");
     if (!b->special || !b->lane_mask || !b->lanes)
       return lbm_err::set(LBM_ERR_ARG, "plan_bind: the in-place step needs the lane-granular lists (special, "
                                        "lane_mask, lanes)");
