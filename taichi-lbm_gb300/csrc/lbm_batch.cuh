@@ -128,14 +128,18 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean_pf(const BatchL
   for (int i = threadIdx.x; i < BATCH_WARPS * TPW; i += BATCH_WARPS * 32) items[i] = tiles[t0 + i].item;
   __syncthreads();
   unsigned char* ring = lean_ring + warp * B::WARP_BYTES;
+  // read once: every cp.async below clobbers memory, which would reload them
+  const uint32_t nseg_mul = p.nseg_mul;
+  const int nseg_shift = p.nseg_shift, nseg = p.nseg;
+  const uint32_t* lane_mask = p.lane_mask;
   // stage the copies of the warp's tile j (none past the last) and commit them as one group
   auto issue = [&](int j) {
     const int item = j < TPW ? items[j * BATCH_WARPS + warp] : -1;
     if (item >= 0) {
       unsigned char* stage = ring + (j % NS) * B::STRIDE;
-      const int y = fast_div(item, p.nseg_mul, p.nseg_shift);
-      stage_issue_row<LeanParams, ST, V, NS>(p, stage, y, (item - y * p.nseg) * 32 * V, lane);
-      cp_async<4>(stage + B::MASK_OFF + lane * 4, p.lane_mask + item);
+      const int y = fast_div(item, nseg_mul, nseg_shift);
+      stage_issue_row<LeanParams, ST, V, NS>(p, stage, y, (item - y * nseg) * 32 * V, lane);
+      cp_async<4>(stage + B::MASK_OFF + lane * 4, lane_mask + item);
     }
     cp_async_commit();
   };
@@ -150,8 +154,8 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_lean_pf(const BatchL
     const unsigned char* stage = ring + (j % NS) * B::STRIDE;
     const uint32_t mask = reinterpret_cast<const uint32_t*>(stage + B::MASK_OFF)[lane];
     if (mask == 0xffffffffu) continue;  // uniform over the warp
-    const int y = fast_div(item, p.nseg_mul, p.nseg_shift);
-    const int x0 = (item - y * p.nseg) * 32 * V + lane * V;
+    const int y = fast_div(item, nseg_mul, nseg_shift);
+    const int x0 = (item - y * nseg) * 32 * V + lane * V;
     float h[V][9];
     stage_gather_row<LeanParams, ST, V, NS>(p, stage, x0, lane, h);
     const bool skip = (mask >> lane) & 1u;

@@ -649,17 +649,23 @@ template <class P, int ST, int V, int NS>
 __device__ __forceinline__ void stage_issue_row(const P& p, unsigned char* stage, int y, int x0s, int lane) {
   using T = typename Storage<ST>::T;
   using G = PfGeom<ST, V, NS>;
-  const int x0 = x0s + lane * V;
-  const bool live = x0 < p.nx;
-  const int ilast = p.nx - 1 - x0;
-  const bool need_right = live && (lane == 31 || (ilast >= 0 && ilast < V));
-  const int xl = x0 > 0 ? x0 - 1 : p.nx - 1;
-  const int xr = x0 + V < p.nx ? x0 + V : 0;
+  // the fields are read once, before the copies: each cp.async clobbers
+  // memory, and the parameters may live in shared memory (batched kernels)
+  const int nx = p.nx;
+  const size_t plane = p.plane, pitch = (size_t)p.pitch;
   const T* src = reinterpret_cast<const T*>(p.src);
+  const int x0 = x0s + lane * V;
+  const bool live = x0 < nx;
+  const int ilast = nx - 1 - x0;
+  const bool need_right = live && (lane == 31 || (ilast >= 0 && ilast < V));
+  const int xl = x0 > 0 ? x0 - 1 : nx - 1;
+  const int xr = x0 + V < nx ? x0 + V : 0;
+  const T* rows[3] = {src + (size_t)wrap(y + 1, p.ny) * pitch, src + (size_t)y * pitch,
+                      src + (size_t)wrap(y - 1, p.ny) * pitch};  // rows y - cy for cy = -1, 0, 1
   uint32_t* edges = reinterpret_cast<uint32_t*>(stage + G::EDGE_OFF);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    const T* row = src + (size_t)k * p.plane + (size_t)wrap(y - CY(k), p.ny) * p.pitch;
+    const T* row = rows[CY(k) + 1] + (size_t)k * plane;
     if (live) cp_async<V * (int)sizeof(T)>(stage + k * G::POP_BYTES + lane * V * (int)sizeof(T), row + x0);
     if (CX(k) == 1 && lane == 0 && live) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xl));
     if (CX(k) == -1 && need_right) cp_async<4>(edges + edge_slot(k) * 32 + lane, edge_word<ST>(row, xr));

@@ -122,13 +122,15 @@ __device__ __forceinline__ void sc_issue(const P& p, unsigned char* ring, int j,
   if (j < nrow) {
     unsigned char* st = ring + (j % sc_slots<ST>()) * G::STAGE_BYTES;
     const int y = wrap(yb - 1 + j, p.ny);
-    stage_issue_row<P, ST, V, sc_slots<ST>()>(p, st, y, x0s, lane);
+    // the halo word's source first: the copies below clobber memory, and the
+    // parameters may live in shared memory (batched strips)
     int k;
     const int xs = sc_halo_column<P, V>(p, x0s, lane, k);
-    if (xs >= 0) {
-      const T* row = reinterpret_cast<const T*>(p.src) + (size_t)k * p.plane + (size_t)wrap(y - cy_dyn(k), p.ny) * p.pitch;
-      cp_async<4>(st + G::ITEM_OFF + lane * 4, edge_word<ST>(row, xs));
-    }
+    const T* row = xs >= 0 ? reinterpret_cast<const T*>(p.src) + (size_t)k * p.plane +
+                                 (size_t)wrap(y - cy_dyn(k), p.ny) * p.pitch
+                           : nullptr;
+    stage_issue_row<P, ST, V, sc_slots<ST>()>(p, st, y, x0s, lane);
+    if (xs >= 0) cp_async<4>(st + G::ITEM_OFF + lane * 4, edge_word<ST>(row, xs));
   }
   cp_async_commit();
 }
