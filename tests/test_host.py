@@ -278,3 +278,71 @@ def test_lane_mask_and_lane_list_cover_exactly_the_special_nodes(V):
     expect = [((y * nseg + s) * 32 + l) for y, s in zip(ys, segs) for l in range(32) if (lm[y, s] >> l) & 1]
     assert sorted(np.asarray(cp.lanes).tolist()) == sorted(expect)
     assert np.array_equal(np.asarray(cp.seg_flags).reshape(ny, nseg) != 0, lm != 0)
+
+
+def _aa_emulation(nx, ny, steps, seed=3):
+    """Ping-pong and in-place (AA-pattern) steps emulated in numpy on a channel
+    periodic in x with solid rows at y = 0 and y = ny - 1 (bounce-back from
+    them), with an arbitrary per-node 'collision'; returns both states."""
+    cx = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+    cy = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+    opp = np.array([0, 3, 4, 1, 2, 7, 8, 5, 6])
+    active = np.ones((nx, ny), bool)
+    active[:, 0] = active[:, ny - 1] = False
+    bounce = np.zeros((9, nx, ny), bool)  # link k of x comes from a solid node
+    for k in range(1, 9):
+        bounce[k] = active & ~np.roll(active, (cx[k], cy[k]), axis=(0, 1))
+    rng = np.random.default_rng(seed)
+    state0 = rng.random((9, nx, ny))
+    perm = np.array([0, 5, 2, 7, 4, 1, 6, 3, 8])
+
+    def collide(f):  # any deterministic function of the node's nine values
+        return 0.5 * f[perm] + 0.25 * f.sum(axis=0, keepdims=True) / 9.0
+
+    def pulled(P):
+        f = np.empty_like(P)
+        for k in range(9):
+            f[k] = np.where(bounce[k], P[opp[k]], np.roll(P[k], (cx[k], cy[k]), axis=(0, 1)))
+        return f
+
+    P = state0.copy()
+    for _ in range(steps):  # ping-pong: pull, collide, store at the node
+        post = collide(pulled(P))
+        P = np.where(active[None], post, P)
+    A = state0.copy()
+    for s in range(steps):
+        if s % 2 == 0:  # phase A: pull; write f*_opp(k) where f_k was read
+            post = collide(pulled(A))
+            out = A.copy()
+            for k in range(9):
+                val = post[opp[k]]
+                # bounced links: read and written at the node itself, slot opp(k)
+                out[opp[k]] = np.where(active & bounce[k], val, out[opp[k]])
+                # streamed links: slot k of x - c_k
+                moved = np.roll(np.where(active & ~bounce[k], val, np.nan), (-cx[k], -cy[k]), axis=(0, 1))
+                out[k] = np.where(np.isnan(moved), out[k], moved)
+            A = out
+        else:  # phase B: f_k at slot opp(k) of the node, f*_k to slot k
+            post = collide(A[opp])
+            A = np.where(active[None], post, A)
+    if steps % 2 == 1:  # swap each streamed pair (slot k of x, slot opp(k) of x + c_k) back
+        out = A.copy()
+        for k in (1, 2, 5, 6):
+            tgt_active = np.roll(active, (-cx[k], -cy[k]), axis=(0, 1))
+            tgt_bounce = np.roll(bounce[k], (-cx[k], -cy[k]), axis=(0, 1))
+            pair = active & tgt_active & ~tgt_bounce
+            other = np.roll(A[opp[k]], (-cx[k], -cy[k]), axis=(0, 1))
+            out[k] = np.where(pair, other, A[k])
+            back = np.roll(np.where(pair, A[k], np.nan), (cx[k], cy[k]), axis=(0, 1))
+            out[opp[k]] = np.where(np.isnan(back), out[opp[k]], back)
+        A = out
+    return P, A
+
+
+@pytest.mark.parametrize("steps", [1, 2, 5, 8])
+def test_in_place_layout_algebra(steps):
+    """The in-place step's two phases and the swap after an odd run leave the
+    buffer holding exactly the ping-pong state (emulated in numpy: reads,
+    writes and bounce-back links as the kernels do them)."""
+    P, A = _aa_emulation(12, 7, steps)
+    assert np.array_equal(P, A)
