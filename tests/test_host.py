@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from tests.cases import ROOT, load_fixture
+from tests.cases import ROOT, fixture_names, load_fixture
 
 
 def header_functions():
@@ -346,3 +346,32 @@ def test_in_place_layout_algebra(steps):
     writes and bounce-back links as the kernels do them)."""
     P, A = _aa_emulation(12, 7, steps)
     assert np.array_equal(P, A)
+
+
+def test_fixtures_compile_in_place():
+    """Every non-Shan-Chen fixture composition passes the in-place checks, and
+    its read sites are exactly the neighbours its NEEM and open boundaries read."""
+    from taichi_lbm import _capi as A
+    from taichi_lbm._plan import READS, compile_plan
+    cx = (0, 1, 0, -1, 0, 1, -1, -1, 1)
+    cy = (0, 0, 1, 0, -1, 1, 1, -1, -1)
+    checked = 0
+    for name in fixture_names():
+        meta, arrays = load_fixture(name)
+        if meta.get("sc"):
+            continue
+        nx, ny = meta["NX"], meta["NY"]
+        items = items_from_fixture(meta, arrays)
+        cp = compile_plan(nx, ny, arrays["g_fluid"], links_from_mask(arrays["mask"]), items, 4, in_place=True)
+        want = set()
+        for it in items:
+            if it.kind not in READS or it.nodes.size == 0:
+                continue
+            _, _, x2_f, x3_f = READS[it.kind]
+            for d, on in ((1, x2_f), (2, x3_f)):
+                if on:
+                    want |= {(int(i) - d * cx[it.direction], int(j) - d * cy[it.direction]) for i, j in it.nodes}
+        got = [tuple(t) for t in cp.read_sites.tolist()]
+        assert got == sorted(want, key=lambda t: (t[1], t[0])), name
+        checked += 1
+    assert checked >= 16
