@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--served-capacity", type=float, default=None, metavar="MLUPS",
                     help="capacity the served stream's arrival rate is 80%% of (default: the single-lattice "
                          "BGK fp16s line)")
+    ap.add_argument("--served-slice", type=int, default=200, help="steps per slice of the served batch")
     ap.add_argument("--served-shape", default=None, metavar="V,SOLO,FORM",
                     help="served batch shape (nodes per thread, solo threshold, lean form) instead of tuning it")
     ap.add_argument("--alone-sample", type=int, default=16,
@@ -323,7 +324,7 @@ def run_batched(tl, storage, K, W, gpu_index, graphs=True):
             "clocks": clk.summary()}
 
 
-def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8, shape=None):
+def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8, shape=None, slice_steps=200):
     """Served request stream: n seeded cylinder-channel requests (sizes
     128..2048 x NX/4, Re 20..200, log-uniform 2k..50k steps, BGK/TRT/MRT, 20%
     power law) arriving as a Poisson process at 80% of the capacity implied by
@@ -349,7 +350,7 @@ def run_served(tl, n, capacity_mlups, gpu_index, storage="fp16s", sample_alone=8
         tuner.batch_shape("served", lambda V: [r.build(tl, nodes_per_thread=V) for r in reqs[:32]], storage)
     tune_s = time.perf_counter() - t0
     torch.cuda.empty_cache()
-    srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=200, builders=4, autotuner=tuner)
+    srv = tl.Server(tl, hbm_budget=64 << 30, graphs=True, slice_steps=slice_steps, builders=4, autotuner=tuner)
     for r in reqs:
         srv.submit(r)
     with Clocks(gpu_index) as clk:
@@ -496,10 +497,10 @@ def run_ours(a):
                          "2048}, NY = NX/4, r = NY/10 at x = NX/5, Re ~ U[20, 200] via tau (u_max 0.04), "
                          "steps log-uniform in [2000, 50000], BGK/TRT/MRT uniform, 20% power law n ~ "
                          f"U[0.5, 1.5]; Poisson arrivals at 80% of a capacity of {cap:.0f} MLUPS; "
-                         f"{a.served_storage} storage, HBM budget 64 GiB, 200-step slices, "
+                         f"{a.served_storage} storage, HBM budget 64 GiB, {a.served_slice}-step slices, "
                          "CUDA graphs; diverged requests are evicted and their updates not counted"},
             **run_served(tl, a.requests, cap, local, storage=a.served_storage, sample_alone=a.alone_sample,
-                         shape=a.served_shape))
+                         shape=a.served_shape, slice_steps=a.served_slice))
     if rank == 0 and ws == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(cfg, a.model, a.cpu_seconds)
     if dist is not None:
