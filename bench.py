@@ -98,6 +98,30 @@ def workload_config(a):
             "cy": CONFIG["cy"] * ny / CONFIG["ny"], "tau": CONFIG["tau"], "umax": CONFIG["umax"]}
 
 
+def arm_config(a, cfg, active, V, ws):
+    """The workload both arms name in their JSON line (the reference arm
+    times a bounded sample of it, described in its cpu_baseline)."""
+    return {"workload": f"cylinder channel {cfg['nx']}x{cfg['ny']}, r={cfg['radius']:g} at "
+                        f"({cfg['cx']:g},{cfg['cy']:g}), {a.model.upper()} tau={cfg['tau']}, "
+                        f"parabolic inlet u_max={cfg['umax']}, PressureNEEM outlet, "
+                        "bounce-back walls", "nodes": cfg["nx"] * cfg["ny"],
+            "updated_nodes_per_step": int(active), "model": a.model, "storage": a.storage,
+            "nodes_per_thread": int(V), "pipeline": a.pipeline, "in_place": a.in_place,
+            "parallelism": f"replicas x{ws}",
+            "l2": ("state (9 populations, one buffer)" if a.in_place else "state (2 x 9 populations)")
+                  + " larger than L2; no flush needed"}
+
+
+def channel_active_nodes(cfg):
+    """Colliding nodes of the channel: every node outside the strict disc,
+    in the f32 arithmetic of BoundaryEngine.Mask_cricle_identify."""
+    import numpy as np
+    x, y, r = np.float32(cfg["cx"]), np.float32(cfg["cy"]), np.float32(cfg["radius"])
+    dx = np.arange(cfg["nx"], dtype=np.float32)[:, None] - x
+    dy = np.arange(cfg["ny"], dtype=np.float32)[None, :] - y
+    return int(cfg["nx"] * cfg["ny"] - np.count_nonzero((dx * dx + dy * dy) < (r * r)))
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -432,15 +456,7 @@ def run_ours(a):
         "warmup": W, "ms_per_step": round(ms / K, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if a.storage == "fp32" else f"f32 compute, {a.storage} storage",
         "data": "synthetic (cylinder channel, rho=1, u=0 start)",
-        "config": {"workload": f"cylinder channel {cfg['nx']}x{cfg['ny']}, r={cfg['radius']:g} at "
-                               f"({cfg['cx']:g},{cfg['cy']:g}), {a.model.upper()} tau={cfg['tau']}, "
-                               f"parabolic inlet u_max={cfg['umax']}, PressureNEEM outlet, "
-                               "bounce-back walls", "nodes": cfg["nx"] * cfg["ny"],
-                   "updated_nodes_per_step": active, "model": a.model, "storage": a.storage,
-                   "nodes_per_thread": solver.V, "pipeline": a.pipeline, "in_place": a.in_place,
-                   "parallelism": f"replicas x{ws}",
-                   "l2": ("state (9 populations, one buffer)" if a.in_place else "state (2 x 9 populations)")
-                         + " larger than L2; no flush needed"},
+        "config": arm_config(a, cfg, active, solver.V, ws),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes_per_launch": BYTES_PER_LU[a.storage] * active,
@@ -557,9 +573,10 @@ def run_reference(a):
     line = {"impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": METRIC,
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": K, "warmup": W,
             "ms_per_step": round(dt / K * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (cylinder channel)",
-            "config": {"workload": f"cylinder channel band {cfg['nx']}x{ny}, {a.model.upper()} "
-                                   f"tau={cfg['tau']}", "model": a.model},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (cylinder channel, rho=1, u=0 start)",
+            "config": arm_config(a, cfg, channel_active_nodes(cfg),
+                                 a.nodes_per_thread or 4,  # FusedSolver's default node width
+                                 int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": round(mlups, 2), "unit": METRIC, "cores": os.cpu_count(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(mlups, 2), "unit": METRIC, "h2d_bytes_per_step": 0,
