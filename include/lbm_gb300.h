@@ -363,7 +363,8 @@ typedef struct LbmPlanDesc {
    * pull step does and writes f*_opp(k)(x) where it read f_k(x); phase B
    * reads f_k(x) from slot opp(k) of x and writes f*_k(x) to slot k of x.
    * A run that ends on phase A swaps the streamed pairs back, so between
-   * runs the buffer holds what the ping-pong state would hold, bit for bit.
+   * runs the buffer holds what the ping-pong state would hold, bit for bit
+   * (that swap is one more pass over the buffer: run many steps per call).
    * Needs the direct pipeline, no Shan-Chen, the lane-granular lists, every
    * bounce-back link cut on both sides (a colliding node that bounces back
    * the population coming from a colliding neighbour is bounced back by it
