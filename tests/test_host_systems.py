@@ -124,3 +124,24 @@ def test_ib_node_placement_matches_reference(built):
     s.IBNodes.force.from_numpy(f)
     IBEngine(1).ComputeParticleForce(s)
     assert np.array_equal(s.Sphere.force.to_numpy()[0], f[0, n - 1])
+
+
+def test_both_bench_arms_name_the_same_workload(built):
+    """The reference arm's JSON line names the workload config of ours; its
+    colliding-node count follows the disc rule of
+    BoundaryEngine.Mask_cricle_identify (f32, strict)."""
+    import types
+
+    import bench
+    import taichi_lbm as tl
+    from taichi_lbm.fields import MaskField
+    args = types.SimpleNamespace(nx=512, ny=128, model="bgk", storage="fp32", pipeline="direct", in_place=False,
+                                 nodes_per_thread=None)
+    cfg = bench.workload_config(args)
+    n = bench.channel_active_nodes(cfg)
+    owner = types.SimpleNamespace(NX=cfg["nx"], NY=cfg["ny"], mask=MaskField(cfg["nx"], cfg["ny"]))
+    tl.BoundaryEngine().Mask_cricle_identify(owner, cfg["cx"], cfg["cy"], cfg["radius"])
+    assert n == int((owner.mask.to_numpy() == 1).sum())
+    ours = bench.arm_config(args, cfg, n, 4, 1)
+    assert ours["updated_nodes_per_step"] == n and ours["nodes"] == 512 * 128
+    assert ours["workload"].startswith("cylinder channel 512x128, r=12.5 at (100,64), BGK")
